@@ -1,0 +1,291 @@
+#!/usr/bin/env python3
+"""Benchmark: cell-steps/s of the Strang-split reacting-Euler step on the 2D H2/O2/Ar
+detonation (2048 x 512 cells, FP64), one GPU per rank.
+
+One "step" is one full Strang step of the whole grid: flow(dt/2) (two Euler stages
+and the Heun combine), react(dt), flow(dt/2), with the CFL dt.  The batched form
+(fused TMA flux kernel + persistent work-queue chemistry) is the headline value;
+the plain form (face/update kernels + one-thread-per-cell chemistry) is timed beside
+it.  `e2e` runs the same steps through the public stepper API with the state in
+pinned HOST memory, copied in and out every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun) every rank runs an independent replica (the reacting step of
+one grid does not shard across these GPUs in this build): value = all ranks' cell-steps
+over the slowest rank's time.  --impl reference times the CPU restatement of the
+reference (the reference itself needs Cantera, SUNDIALS and AMReX, absent here) on
+this host's cores over a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s, 2D H2 detonation FP64: batched vs plain GPU; adjoint/forward time"
+NX, NY = 2048, 512
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=8)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--plain-steps", type=int, default=None, help="steps timed for the plain form (default: steps)")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cfl", type=float, default=0.5)
+    p.add_argument("--nx", type=int, default=NX)
+    p.add_argument("--ny", type=int, default=NY)
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------ CPU (oracle) leg
+def cpu_sample(steps=2, warm=1, rows=4, threads=0, nx=NX):
+    """Oracle Strang steps on a periodic strip (nx x rows) of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from hyperflow_gb300 import workloads as W
+    oracle.build()
+    oracle.set_species(10)
+    U, lvd = W.det2d(seed=0, diluent="AR", nx=nx, ny=rows)
+    g = oracle.make_grid(nx, rows, 1e-4, 1e-4, periodic=(0, 1), bc_lo=(0, 0), bc_hi=(1, 0), inlet=lvd["inlet"])
+    Ug = oracle.ghosted(U.transpose(1, 2, 0))
+    for _ in range(warm):
+        dt = oracle.cfl_dt(g, Ug, 0.5)
+        Ug, _, st, _ = oracle.strang_step(g, Ug, dt, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = oracle.cfl_dt(g, Ug, 0.5)
+        Ug, _, st, _ = oracle.strang_step(g, Ug, dt, threads=threads)
+        if st:
+            raise RuntimeError("oracle step failed")
+    el = time.perf_counter() - t0
+    cores = threads or os.cpu_count()
+    return {"value": nx * rows * steps / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d Strang steps (after %d warm-up) of a %dx%d periodic strip of the 2D detonation; "
+                      "serial flux loop, OpenMP dynamic,8 chemistry (the reference's threading)" % (steps, warm, nx, rows),
+            "seconds": el}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    per = []
+    for _ in range(args.warmup):
+        pass
+    cb = cpu_sample(steps=max(1, args.steps // 4), warm=1, rows=4, nx=args.nx)
+    line = {"metric": METRIC, "value": cb["value"], "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * args.nx * args.ny / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "2D H2/O2/Ar detonation %dx%d, 64-column hot band, periodic y" % (args.nx, args.ny),
+                       "cells": args.nx * args.ny},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (Cantera/SUNDIALS/AMReX) cannot be built here; this arm times the CPU "
+                    "restatement of its path"}
+    print(json.dumps(line), flush=True)
+    del per
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import workloads as W
+    U0, lvd = W.det2d(seed=rank, diluent="AR", nx=args.nx, ny=args.ny)
+    ctx = hf.Context("H2_Li+AR", device=local)
+    level = hf.make_level(**lvd)
+    cells = args.nx * args.ny
+    nv = U0.shape[0]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(flux, chem, steps, warmup, timing=False, clocks=None):
+        st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=flux, chem=chem)
+        for _ in range(warmup):
+            st.step(cfl=args.cfl)
+        c0 = ctx.counters()
+        if timing:
+            ctx.set_timing(True)
+        barrier()
+        if clocks:
+            clocks.start()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(steps):
+            st.step(cfl=args.cfl)
+            flush.zero_()
+        ev1.record()
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        ck = clocks.stop() if clocks else None
+        tm = ctx.timing() if timing else None
+        if timing:
+            ctx.set_timing(False)
+        c1 = ctx.counters()
+        st.close()
+        return max_over_ranks(ms), ck, tm, {k: c1[k] - c0[k] for k in c1}
+
+    clocks = Clocks(local)
+    ms, ck, tm, cnt = timed("fused", "persistent", args.steps, args.warmup, timing=True, clocks=clocks)
+    value = world * cells * args.steps / (ms * 1e-3)
+    plain = None
+    if not args.no_plain:
+        ps = args.plain_steps or args.steps
+        pms, _, ptm, pcnt = timed("plain", "plain", ps, args.warmup, timing=True)
+        plain = {"value": world * cells * ps / (pms * 1e-3), "ms_per_step": pms / ps, "steps": ps,
+                 "chem_ms_per_step": ptm["chem"][0] / ps, "flux_ms_per_step": ptm["flux"][0] / ps}
+
+    e2e = None
+    if not args.no_e2e:
+        st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux="fused", chem="persistent")
+        host = torch.from_numpy(U0.copy()).pin_memory()
+        for _ in range(args.warmup):
+            st.set_host(host)
+            st.step(cfl=args.cfl)
+            st.get_host(host)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st.set_host(host)
+            st.step(cfl=args.cfl)
+            st.get_host(host)
+        barrier()
+        el = max_over_ranks(time.perf_counter() - t0)
+        st.close()
+        nbytes = nv * cells * 8
+        e2e = {"value": world * cells * args.steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    pk = peaks()
+    chem_ms, chem_n = tm["chem"]
+    bytes_per_launch = 2 * nv * 8 * cells  # read and write every cell state once
+    achieved = bytes_per_launch / (chem_ms / max(chem_n, 1) * 1e-3) / 1e9
+    hbm = pk.get("hbm_gbs", 6800.0)
+    roof = {"kernel": "k_chem_persistent", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
+            "note": "the chemistry kernel is FP64-pipe bound, not HBM bound; the HBM fraction is reported per "
+                    "the contract, the FP64 figures are in profiles/"}
+    cpu = None
+    if not args.no_cpu:
+        cb = cpu_sample(steps=2, warm=1, rows=4, nx=args.nx)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "2D H2/O2/Ar detonation %dx%d, 64-column hot band at 40 atm/3000 K, +-1%% density "
+                               "perturbation, periodic y, CFL %.2f" % (args.nx, args.ny, args.cfl),
+                   "cells": cells, "species": 10, "mechanism": "H2_Li + inert AR extension",
+                   "chem_tolerances": "rtol 1e-8 atol 1e-15", "form": "fused flux + persistent chemistry",
+                   "l2": "256 MB buffer written between timed steps; state buffers 109 MB each x4",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "clocks": ck, "e2e": e2e, "gpu_launches": cnt["kernel_launches"],
+        "breakdown_ms_per_step": {"flux": tm["flux"][0] / args.steps, "chem": tm["chem"][0] / args.steps,
+                                  "other": tm["other"][0] / args.steps},
+        "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
+        "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
+        "roofline": roof, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,12 @@
+"""GB300-native reacting-Euler step of HyperFlow V3 (flux, ghost fill, chemistry).
+
+The compute path is libhyperflow_gpu.so (hand-written CUDA for sm_103a behind the
+C ABI of include/hyperflow_gpu.h); this package binds it with ctypes and keeps the
+reference's per-block names (see solver.py).  There is no CPU fallback.
+"""
+from .solver import (ChemistryBatch, ConservativeInterp, Context, DomainError, HyperFlowError, PatchArray,  # noqa
+                     Stepper, admissible, cfl_dt, euler_stage, fill, hllc, make_level, properties, validate)
+
+__all__ = ["ChemistryBatch", "ConservativeInterp", "Context", "DomainError", "HyperFlowError", "PatchArray",
+           "Stepper", "admissible", "cfl_dt", "euler_stage", "fill", "hllc", "make_level", "properties",
+           "validate"]

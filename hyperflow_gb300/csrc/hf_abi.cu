@@ -1,0 +1,460 @@
+// C ABI of libhyperflow_gpu.so (declared in include/hyperflow_gpu.h): context,
+// scratch management, status read-back and dispatch to the kernels of hf_flux.cu
+// and hf_chem.cu.  Error behaviour mirrors the reference's exceptions as return
+// codes (see the header for the mapping).
+#include <cuda.h>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "hf_internal.h"
+#include "mech_h2li.h"
+
+using namespace hf;
+
+struct hf_ctx {
+    int ns = 9;
+    int device = 0;
+    int sm_count = 1;
+    std::string err;
+    hf_counters cnt{};
+    DevStatus* st = nullptr;       // device status block
+    DevStatus* st_host = nullptr;  // pinned mirror
+    void* scratch = nullptr;       // grown on demand
+    size_t scratch_bytes = 0;
+    hf_patch* d_patches = nullptr;
+    int d_patch_cap = 0;
+    // tensor-map cache for the fused flux kernel
+    struct TMap { const double* base; hf_patch P; alignas(64) unsigned char map[128]; };
+    std::vector<TMap> tmaps;
+    // optional per-class device timing
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool pending = false;
+    int pending_class = 0;
+    double ms[3] = {0, 0, 0};
+    int64_t launches[3] = {0, 0, 0};
+};
+
+namespace {
+
+hf_status fail(hf_ctx* c, hf_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+hf_status cuda_fail(hf_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, HF_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define HF_CUDA(call)                                             \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+cudaError_t reset_status(hf_ctx* ctx, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(ctx->st, 0, sizeof(DevStatus), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(&ctx->st->bad_cell, 0xff, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(&ctx->st->donor[0], 0xff, sizeof(ctx->st->donor), s);
+}
+// Timing brackets: tic() before a class's launches, toc() after them; the elapsed
+// time is collected at the next stream synchronisation (read_status).
+void tic(hf_ctx* ctx, int cls, cudaStream_t s) {
+    if (!ctx->timing) return;
+    cudaEventRecord(ctx->ev0, s);
+    ctx->pending_class = cls;
+}
+void toc(hf_ctx* ctx, cudaStream_t s, int64_t nlaunch) {
+    if (!ctx->timing) return;
+    cudaEventRecord(ctx->ev1, s);
+    ctx->pending = true;
+    ctx->launches[ctx->pending_class] += nlaunch;
+}
+cudaError_t read_status(hf_ctx* ctx, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && ctx->pending) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->ms[ctx->pending_class] += t;
+        ctx->pending = false;
+    }
+    return e;
+}
+void* scratch(hf_ctx* ctx, size_t bytes) {
+    if (bytes > ctx->scratch_bytes) {
+        if (ctx->scratch) cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        if (cudaMalloc(&ctx->scratch, bytes) != cudaSuccess) return nullptr;
+        ctx->scratch_bytes = bytes;
+    }
+    return ctx->scratch;
+}
+cudaError_t upload_patches(hf_ctx* ctx, const hf_patch* p, int n, cudaStream_t s) {
+    if (n > ctx->d_patch_cap) {
+        if (ctx->d_patches) cudaFree(ctx->d_patches);
+        ctx->d_patches = nullptr;
+        cudaError_t e = cudaMalloc(&ctx->d_patches, sizeof(hf_patch) * n);
+        if (e != cudaSuccess) return e;
+        ctx->d_patch_cap = n;
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->d_patches, p, sizeof(hf_patch) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+bool patch_ok(const hf_patch& P) {
+    return P.nx > 0 && P.ny > 0 && P.ng >= 2 && P.pitch >= P.nx + 2 * P.ng &&
+           P.comp_stride >= P.pitch * (P.ny + 2 * P.ng) && P.offset >= 0;
+}
+bool level_ok(const hf_level& L) {
+    if (L.nx <= 0 || L.ny <= 0 || !(L.dx > 0) || !(L.dy > 0)) return false;
+    for (int d = 0; d < 2; ++d) {
+        if (L.bc_lo[d] < 0 || L.bc_lo[d] > 3 || L.bc_hi[d] < 0 || L.bc_hi[d] > 2) return false;
+        if (L.bc_lo[d] == HF_BC_WEDGE && (d != 1 || L.periodic[1])) return false;
+    }
+    return true;
+}
+const void* tensor_map(hf_ctx* ctx, const double* base, const hf_patch& P) {
+    for (auto& t : ctx->tmaps)
+        if (t.base == base && !memcmp(&t.P, &P, sizeof(P))) return t.map;
+    hf_ctx::TMap t;
+    t.base = base;
+    t.P = P;
+    if (!make_tensor_map(t.map, base, P, ctx->ns + 3)) return nullptr;
+    if (ctx->tmaps.size() > 64) ctx->tmaps.erase(ctx->tmaps.begin());
+    ctx->tmaps.push_back(t);
+    return ctx->tmaps.back().map;
+}
+
+}  // namespace
+
+namespace hf {
+void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries) {
+    ctx->cnt.first_order_stages += first_order_stages;
+    ctx->cnt.retries += retries;
+}
+}  // namespace hf
+
+extern "C" {
+
+hf_status hf_init(const char* mechanism, int device, hf_ctx** out) {
+    if (!out) return HF_ERR_ARG;
+    *out = nullptr;
+    int ns = 9;
+    if (mechanism && *mechanism) {
+        std::string m(mechanism);
+        auto ends = [&](const std::string& suf) {
+            return m.size() >= suf.size() && m.compare(m.size() - suf.size(), suf.size(), suf) == 0;
+        };
+        if (m == "H2_Li" || ends("H2_Li.yaml")) ns = 9;
+        else if (m == "H2_Li+AR") ns = 10;
+        else return HF_ERR_ARG;
+    }
+    hf_ctx* ctx = new hf_ctx();
+    ctx->ns = ns;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->st, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->st_host, sizeof(DevStatus));
+    if (e == cudaSuccess) e = chem_set_rate_scale(nullptr);
+    if (e != cudaSuccess) {
+        hf_destroy(ctx);
+        return HF_ERR_CUDA;
+    }
+    *out = ctx;
+    return HF_OK;
+}
+
+void hf_set_timing(hf_ctx* ctx, int enable) {
+    if (!ctx) return;
+    if (enable && !ctx->ev0) {
+        cudaEventCreate(&ctx->ev0);
+        cudaEventCreate(&ctx->ev1);
+    }
+    ctx->timing = enable != 0 && ctx->ev0;
+    ctx->pending = false;
+    for (int k = 0; k < 3; ++k) { ctx->ms[k] = 0; ctx->launches[k] = 0; }
+}
+void hf_get_timing(const hf_ctx* ctx, double ms[3], int64_t launches[3]) {
+    for (int k = 0; k < 3; ++k) {
+        if (ms) ms[k] = ctx ? ctx->ms[k] : 0.0;
+        if (launches) launches[k] = ctx ? ctx->launches[k] : 0;
+    }
+}
+
+void hf_destroy(hf_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->st) cudaFree(ctx->st);
+    if (ctx->st_host) cudaFreeHost(ctx->st_host);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->d_patches) cudaFree(ctx->d_patches);
+    delete ctx;
+}
+
+int hf_nspecies(const hf_ctx* ctx) { return ctx ? ctx->ns : 0; }
+const char* hf_last_error(const hf_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void hf_get_counters(const hf_ctx* ctx, hf_counters* out) {
+    if (ctx && out) *out = ctx->cnt;
+}
+
+hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale) {
+    if (!ctx) return HF_ERR_ARG;
+    HF_CUDA(cudaSetDevice(ctx->device));
+    HF_CUDA(chem_set_rate_scale(scale));
+    return HF_OK;
+}
+
+hf_status hf_properties(hf_ctx* ctx, const double* q, int64_t stride, int64_t count, double* p, double* a, double* T,
+                        int32_t* status, void* stream) {
+    if (!ctx || !q || !p || !a || !T || !status || count < 0 || stride < count) return fail(ctx, HF_ERR_ARG, "properties: bad arguments");
+    if (count == 0) return HF_OK;
+    HF_CUDA(reset_status(ctx, S(stream)));
+    HF_CUDA(launch_properties(ctx->ns, q, stride, count, p, a, T, status, ctx->st, S(stream), &ctx->cnt.kernel_launches));
+    HF_CUDA(read_status(ctx, S(stream)));
+    return ctx->st_host->flags ? HF_ERR_INADMISSIBLE : HF_OK;
+}
+
+hf_status hf_hllc(hf_ctx* ctx, const double* l, const double* r, const double* pl, const double* pr, int64_t stride,
+                  int64_t count, int dir, double* f, void* stream) {
+    if (!ctx || !l || !r || !pl || !pr || !f || count < 0 || stride < count || (dir != 0 && dir != 1))
+        return fail(ctx, HF_ERR_ARG, "hllc: bad arguments");
+    if (count == 0) return HF_OK;
+    HF_CUDA(launch_hllc(ctx->ns, l, r, pl, pr, stride, count, dir, f, S(stream), &ctx->cnt.kernel_launches));
+    return HF_OK;
+}
+
+hf_status hf_fill_ghosts(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, double* U,
+                         void* stream) {
+    if (!ctx || !level || !patches || npatch <= 0 || !U || !level_ok(*level)) return fail(ctx, HF_ERR_ARG, "fill_ghosts: bad arguments");
+    for (int p = 0; p < npatch; ++p)
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "fill_ghosts: bad patch");
+    HF_CUDA(upload_patches(ctx, patches, npatch, S(stream)));
+    const Level L = make_level(*level);
+    HF_CUDA(launch_fill(ctx->ns, L, patches, ctx->d_patches, npatch, U, S(stream), &ctx->cnt.kernel_launches));
+    return HF_OK;
+}
+
+hf_status hf_interp_coarse_to_fine(hf_ctx* ctx, const hf_patch* coarse, const double* Uc, const hf_patch* fine,
+                                   double* Uf, const int32_t region[4], void* stream) {
+    if (!ctx || !coarse || !Uc || !fine || !Uf || !region || !patch_ok(*coarse) || !patch_ok(*fine))
+        return fail(ctx, HF_ERR_ARG, "interp: bad arguments");
+    if (region[2] < region[0] || region[3] < region[1]) return fail(ctx, HF_ERR_ARG, "interp: empty region");
+    // the coarsened region grown by one must lie in the coarse patch's ghosted box,
+    // the region itself in the fine patch's ghosted box
+    const int ci0 = (region[0] >> 1) - 1, cj0 = (region[1] >> 1) - 1, ci1 = (region[2] >> 1) + 1, cj1 = (region[3] >> 1) + 1;
+    if (ci0 < coarse->ilo - coarse->ng || cj0 < coarse->jlo - coarse->ng || ci1 >= coarse->ilo + coarse->nx + coarse->ng ||
+        cj1 >= coarse->jlo + coarse->ny + coarse->ng)
+        return fail(ctx, HF_ERR_ARG, "interp: coarse patch does not hold the coarsened region");
+    if (region[0] < fine->ilo - fine->ng || region[1] < fine->jlo - fine->ng || region[2] >= fine->ilo + fine->nx + fine->ng ||
+        region[3] >= fine->jlo + fine->ny + fine->ng)
+        return fail(ctx, HF_ERR_ARG, "interp: region outside the fine patch");
+    HF_CUDA(launch_interp(ctx->ns, *coarse, Uc, *fine, Uf, region, S(stream), &ctx->cnt.kernel_launches));
+    return HF_OK;
+}
+
+// Roundoff repair + validation of one level after a stage (BlockAMR.cpp:257, 299-334).
+static hf_status repair_and_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, double* U,
+                                     cudaStream_t s, int64_t* bad_cell) {
+    const double vol = level->dx * level->dy;
+    HF_CUDA(reset_status(ctx, s));
+    int64_t base = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        base = 0;
+        for (int p = 0; p < npatch; ++p) {
+            HF_CUDA(launch_repair_scan(ctx->ns, patches[p], U, base, pass, ctx->st, s, &ctx->cnt.kernel_launches));
+            base += (int64_t)patches[p].nx * patches[p].ny;
+        }
+    }
+    for (int p = 0; p < npatch; ++p)
+        HF_CUDA(launch_repair_apply(ctx->ns, patches[p], U, vol, ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(upload_patches(ctx, patches, npatch, s));
+    HF_CUDA(launch_donor_fix(ctx->ns, ctx->d_patches, npatch, U, vol, ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags & ST_MATERIAL) return fail(ctx, HF_ERR_NEGATIVE, "materially negative species after a stage");
+    ctx->cnt.roundoff_repairs += (int64_t)ctx->st_host->repairs;
+    HF_CUDA(reset_status(ctx, s));
+    base = 0;
+    for (int p = 0; p < npatch; ++p) {
+        HF_CUDA(launch_validate(ctx->ns, patches[p], U, base, ctx->st, s, &ctx->cnt.kernel_launches));
+        base += (int64_t)patches[p].nx * patches[p].ny;
+    }
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags) {
+        if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;
+        return fail(ctx, HF_ERR_INADMISSIBLE, "inadmissible state after a stage");
+    }
+    return HF_OK;
+}
+
+hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U_in,
+                         const double* U_old, double* U_out, double* fx, double* fy, double h, int first_order,
+                         int form, int64_t* bad_cell, void* stream) {
+    if (bad_cell) *bad_cell = -1;
+    if (!ctx || !level || !patches || npatch <= 0 || !U_in || !U_out || U_in == U_out || !level_ok(*level) ||
+        !(h > 0) || (form != HF_FLUX_PLAIN && form != HF_FLUX_FUSED))
+        return fail(ctx, HF_ERR_ARG, "flux_update: bad arguments");
+    for (int p = 0; p < npatch; ++p)
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "flux_update: bad patch");
+    const cudaStream_t s = S(stream);
+    const Level L = make_level(*level);
+    const int nv = ctx->ns + 3;
+    if (form == HF_FLUX_FUSED) {
+        const hf_patch& P = patches[0];
+        if (npatch != 1 || P.ilo != 0 || P.jlo != 0 || P.nx != level->nx || P.ny != level->ny || (P.ng & 1) || fx || fy)
+            return fail(ctx, HF_ERR_ARG, "flux_update: the fused form takes one domain-covering patch, even ng, no face output");
+    }
+    // face flux storage for the plain form
+    int64_t nfx_tot = 0, nfy_tot = 0;
+    for (int p = 0; p < npatch; ++p) {
+        nfx_tot += (int64_t)nv * (patches[p].nx + 1) * patches[p].ny;
+        nfy_tot += (int64_t)nv * patches[p].nx * (patches[p].ny + 1);
+    }
+    double* FX = fx;
+    double* FY = fy;
+    if (form == HF_FLUX_PLAIN && (!fx || !fy)) {
+        double* w = static_cast<double*>(scratch(ctx, sizeof(double) * (size_t)(nfx_tot + nfy_tot)));
+        if (!w) return fail(ctx, HF_ERR_CUDA, "flux_update: scratch allocation failed");
+        if (!FX) FX = w;
+        if (!FY) FY = w + nfx_tot;
+    }
+    auto run = [&](const double* uold) -> hf_status {
+        HF_CUDA(reset_status(ctx, s));
+        const int64_t l0 = ctx->cnt.kernel_launches;
+        tic(ctx, 0, s);
+        if (form == HF_FLUX_FUSED) {
+            const void* tm = tensor_map(ctx, U_in, patches[0]);
+            if (!tm) return fail(ctx, HF_ERR_ARG, "flux_update: TMA descriptor rejected (alignment/pitch)");
+            HF_CUDA(launch_flux_fused(ctx->ns, L, patches[0], tm, U_in, uold, U_out, h, first_order, 0, ctx->st, s,
+                                      &ctx->cnt.kernel_launches));
+        } else {
+            int64_t base = 0, ox = 0, oy = 0;
+            for (int p = 0; p < npatch; ++p) {
+                const hf_patch& P = patches[p];
+                HF_CUDA(launch_flux_plain(ctx->ns, L, P, p, U_in, uold, U_out, FX + ox, FY + oy, h, first_order, base,
+                                          ctx->st, s, &ctx->cnt.kernel_launches));
+                base += (int64_t)P.nx * P.ny;
+                ox += (int64_t)nv * (P.nx + 1) * P.ny;
+                oy += (int64_t)nv * P.nx * (P.ny + 1);
+            }
+        }
+        toc(ctx, s, ctx->cnt.kernel_launches - l0);
+        HF_CUDA(read_status(ctx, s));
+        return HF_OK;
+    };
+    hf_status r = run(U_old);
+    if (r != HF_OK) return r;
+    unsigned f = ctx->st_host->flags;
+    if (bad_cell && f) *bad_cell = (int64_t)ctx->st_host->bad_cell;
+    if (f & ST_TIMEOUT) return fail(ctx, HF_ERR_TIMEOUT, "flux_update: TMA wait timed out");
+    if (f & ST_FACE_BAD) return fail(ctx, HF_ERR_FACE, "flux_update: inadmissible cell state at a face");
+    if (f & ST_STAGE_BAD) return fail(ctx, HF_ERR_INADMISSIBLE, "flux_update: inadmissible stage output");
+    if (f & ST_NEGATIVE) {
+        // roundoff repair path: recompute the pure stage output if it was combined
+        if (U_old) {
+            r = run(nullptr);
+            if (r != HF_OK) return r;
+        }
+        r = repair_and_validate(ctx, level, patches, npatch, U_out, s, bad_cell);
+        if (r != HF_OK) return r;
+        if (U_old) {
+            HF_CUDA(reset_status(ctx, s));
+            int64_t base = 0;
+            for (int p = 0; p < npatch; ++p) {
+                HF_CUDA(launch_combine(ctx->ns, patches[p], U_old, U_out, base, ctx->st, s, &ctx->cnt.kernel_launches));
+                base += (int64_t)patches[p].nx * patches[p].ny;
+            }
+            HF_CUDA(read_status(ctx, s));
+            if (ctx->st_host->flags) {
+                if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;
+                return fail(ctx, HF_ERR_COMBINE, "flux_update: inadmissible Heun combination");
+            }
+        }
+        return HF_OK;
+    }
+    if (f & ST_COMBINE_BAD) return fail(ctx, HF_ERR_COMBINE, "flux_update: inadmissible Heun combination");
+    return HF_OK;
+}
+
+hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index, int64_t count,
+                          double dt, const double* dt_cell, double rtol, double atol, int form, int64_t* first_failed,
+                          void* stream) {
+    if (first_failed) *first_failed = -1;
+    if (!ctx || !U || count < 0 || (!cell_index && comp_stride < count) || (!dt_cell && (!(dt > 0) || !std::isfinite(dt))) ||
+        !(rtol > 0) || !(atol > 0) || (form != HF_CHEM_PLAIN && form != HF_CHEM_PERSISTENT))
+        return fail(ctx, HF_ERR_ARG, "chem_advance: invalid batch extent, interval or tolerances");
+    if (count == 0) return HF_OK;
+    const cudaStream_t s = S(stream);
+    const int nv = ctx->ns + 3;
+    const size_t need = sizeof(double) * (size_t)nv * count + sizeof(int) * (size_t)count;
+    char* w = static_cast<char*>(scratch(ctx, need));
+    if (!w) return fail(ctx, HF_ERR_CUDA, "chem_advance: scratch allocation failed");
+    double* trial = reinterpret_cast<double*>(w);
+    int* failv = reinterpret_cast<int*>(w + sizeof(double) * (size_t)nv * count);
+    HF_CUDA(reset_status(ctx, s));
+    tic(ctx, 1, s);
+    HF_CUDA(launch_chem(ctx->ns, form, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, trial, failv, ctx->st,
+                        ctx->sm_count, s, &ctx->cnt.kernel_launches));
+    toc(ctx, s, 1);
+    HF_CUDA(read_status(ctx, s));
+    ctx->cnt.chem_steps += (int64_t)ctx->st_host->steps;
+    const unsigned f = ctx->st_host->flags;
+    if (f & (ST_CHEM_FAIL | ST_MAXSTEPS)) {
+        if (first_failed) *first_failed = (int64_t)ctx->st_host->bad_cell;
+        char msg[96];
+        snprintf(msg, sizeof msg, "chemistry cell %lld: %s", (long long)ctx->st_host->bad_cell,
+                 (f & ST_MAXSTEPS) && !(f & ST_CHEM_FAIL) ? "step limit" : "integration failed");
+        return fail(ctx, (f & ST_CHEM_FAIL) ? HF_ERR_CHEM_FAIL : HF_ERR_MAXSTEPS, msg);
+    }
+    HF_CUDA(launch_chem_commit(ctx->ns, U, comp_stride, cell_index, count, trial, s, &ctx->cnt.kernel_launches));
+    ctx->cnt.chem_cell_calls += count;
+    return HF_OK;
+}
+
+hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U, double cfl,
+                    double* dt, void* stream) {
+    if (!ctx || !level || !patches || npatch <= 0 || !U || !dt || !(cfl > 0) || !level_ok(*level))
+        return fail(ctx, HF_ERR_ARG, "cfl_dt: bad arguments");
+    const cudaStream_t s = S(stream);
+    const Level L = make_level(*level);
+    HF_CUDA(reset_status(ctx, s));
+    tic(ctx, 2, s);
+    for (int p = 0; p < npatch; ++p)
+        HF_CUDA(launch_cfl(ctx->ns, L, patches[p], U, ctx->st, s, &ctx->cnt.kernel_launches));
+    toc(ctx, s, npatch);
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags) return fail(ctx, HF_ERR_INADMISSIBLE, "cfl_dt: inadmissible cell");
+    double rate;
+    memcpy(&rate, &ctx->st_host->rate_bits, sizeof rate);
+    *dt = cfl / rate;
+    return HF_OK;
+}
+
+hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U,
+                      int64_t* bad_cell, void* stream) {
+    if (bad_cell) *bad_cell = -1;
+    if (!ctx || !level || !patches || npatch <= 0 || !U) return fail(ctx, HF_ERR_ARG, "validate: bad arguments");
+    const cudaStream_t s = S(stream);
+    HF_CUDA(reset_status(ctx, s));
+    tic(ctx, 2, s);
+    int64_t base = 0;
+    for (int p = 0; p < npatch; ++p) {
+        HF_CUDA(launch_validate(ctx->ns, patches[p], U, base, ctx->st, s, &ctx->cnt.kernel_launches));
+        base += (int64_t)patches[p].nx * patches[p].ny;
+    }
+    toc(ctx, s, npatch);
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags) {
+        if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;
+        return fail(ctx, HF_ERR_INADMISSIBLE, "validate: inadmissible cell");
+    }
+    return HF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+// Internal declarations shared by the translation units of libhyperflow_gpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/hyperflow_gpu.h"
+
+namespace hf {
+
+// Device-side status of one stage / reduction launch.
+struct DevStatus {
+    unsigned int flags;
+    unsigned int pad;
+    unsigned long long bad_cell;   // lowest failing linear index (atomicMin), ~0 = none
+    unsigned long long rate_bits;  // CFL: max rate as the bits of a non-negative double
+    unsigned long long counter;    // work-queue head / generic counter
+    unsigned long long steps;      // integrator steps (accepted + rejected)
+    double deficit[16];            // roundoff repair deficits per species
+    unsigned long long peak_bits[16];
+    unsigned long long donor[16];
+    unsigned long long repairs;
+};
+enum : unsigned int {
+    ST_STAGE_BAD = 1u,    // a stage output cell is inadmissible
+    ST_NEGATIVE = 2u,     // a stage output cell has a negative partial density
+    ST_COMBINE_BAD = 4u,  // a Heun-combined cell is inadmissible
+    ST_FACE_BAD = 8u,     // a face fell back to an inadmissible cell state
+    ST_MATERIAL = 16u,    // negative species beyond roundoff (repairRoundoff throws)
+    ST_TIMEOUT = 32u,     // a bounded wait gave up
+    ST_CHEM_FAIL = 64u,
+    ST_MAXSTEPS = 128u,
+    ST_BAD_INPUT = 256u,
+};
+
+struct Level {  // device copy of hf_level
+    int nx, ny;
+    int periodic[2], lo[2], hi[2];
+    double dx, dy, xlo, ylo, wedge_start;
+    double inlet[13];
+};
+inline Level make_level(const hf_level& l) {
+    Level d{};
+    d.nx = l.nx; d.ny = l.ny;
+    for (int k = 0; k < 2; ++k) { d.periodic[k] = l.periodic[k]; d.lo[k] = l.bc_lo[k]; d.hi[k] = l.bc_hi[k]; }
+    d.dx = l.dx; d.dy = l.dy; d.xlo = l.xlo; d.ylo = l.ylo; d.wedge_start = l.wedge_start;
+    for (int n = 0; n < 13; ++n) d.inlet[n] = l.inlet[n];
+    return d;
+}
+
+// Counter updates from the host stepper (hf_abi.cu)
+void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries);
+
+// Launch wrappers (hf_flux.cu)
+cudaError_t launch_fill(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
+                        int npatch, double* U, cudaStream_t s, int64_t* launches);
+cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int pidx, const double* Uin,
+                              const double* Uold, double* Uout, double* fx, double* fy, double h,
+                              int first_order, int64_t cell_base, DevStatus* st, cudaStream_t s,
+                              int64_t* launches);
+cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
+                              const double* Uold, double* Uout, double h, int first_order,
+                              int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches);
+bool make_tensor_map(void* tmap, const double* base, const hf_patch& P, int nv);
+cudaError_t launch_combine(int ns, const hf_patch& P, const double* Uold, double* U, int64_t cell_base,
+                           DevStatus* st, cudaStream_t s, int64_t* launches);
+cudaError_t launch_validate(int ns, const hf_patch& P, const double* U, int64_t cell_base, DevStatus* st,
+                            cudaStream_t s, int64_t* launches);
+cudaError_t launch_cfl(int ns, const Level& L, const hf_patch& P, const double* U, DevStatus* st,
+                       cudaStream_t s, int64_t* launches);
+cudaError_t launch_repair_scan(int ns, const hf_patch& P, const double* U, int64_t cell_base, int pass,
+                               DevStatus* st, cudaStream_t s, int64_t* launches);
+cudaError_t launch_repair_apply(int ns, const hf_patch& P, double* U, double vol, DevStatus* st,
+                                cudaStream_t s, int64_t* launches);
+cudaError_t launch_donor_fix(int ns, const hf_patch* patches_dev, int npatch, double* U, double vol,
+                             DevStatus* st, cudaStream_t s, int64_t* launches);
+cudaError_t launch_properties(int ns, const double* q, int64_t stride, int64_t count, double* p, double* a,
+                              double* T, int32_t* status, DevStatus* st, cudaStream_t s, int64_t* launches);
+cudaError_t launch_hllc(int ns, const double* l, const double* r, const double* pl, const double* pr,
+                        int64_t stride, int64_t count, int dir, double* f, cudaStream_t s, int64_t* launches);
+cudaError_t launch_interp(int ns, const hf_patch& C, const double* Uc, const hf_patch& F, double* Uf,
+                          const int32_t* region, cudaStream_t s, int64_t* launches);
+
+// Chemistry (hf_chem.cu)
+cudaError_t chem_set_rate_scale(const double* scale);
+cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const int64_t* cell_index,
+                        int64_t count, double dt, const double* dt_cell, double rtol, double atol,
+                        double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
+                        int64_t* launches);
+cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
+                               int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
+
+}  // namespace hf

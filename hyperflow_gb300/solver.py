@@ -1,0 +1,331 @@
+"""Python mirror of the reference's per-block interface over the C ABI.
+
+Names follow HyperFlow V3: ``properties``/``admissible``/``hllc``
+(src/physics.cpp:4-48), ``ChemistryBatch.advance`` (src/chemistry_batch.cpp:21-50),
+``fill`` / ``FlowBoundary`` (src/BlockAMR.cpp:137-146, src/FlowBoundary.hpp),
+``ConservativeInterp.interp`` (src/ConservativeInterp.cpp), and a ``Stepper``
+running the loop body of ``BlockAMR::run`` (src/BlockAMR.cpp:409-419).  Errors
+raise like the reference: ``DomainError`` where it throws std::domain_error,
+``RuntimeError`` for a failed chemistry cell ("chemistry cell k: ...").
+
+Device data are torch float64 CUDA tensors used as plain memory: states are
+structure-of-arrays, shape (NV, ...), NV = NS + 3, component order
+rhoY_0..rhoY_{NS-1}, rho*u, rho*v, rho*E (src/solver.hpp:17-25).
+"""
+import ctypes
+
+import torch
+
+from . import _lib as L
+
+SPECIES = ["H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2", "AR"]
+BC = {"reflecting": L.HF_BC_REFLECTING, "transmissive": L.HF_BC_TRANSMISSIVE, "inflow": L.HF_BC_INFLOW,
+      "wedge": L.HF_BC_WEDGE}
+
+
+class HyperFlowError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (L.STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class DomainError(HyperFlowError):
+    """std::domain_error of the reference (inadmissible state)."""
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _need_cuda64(t, name):
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64):
+        raise TypeError("%s must be a float64 CUDA tensor" % name)
+
+
+class Context:
+    """hf_init/hf_destroy: one mechanism on one device (src/BlockAMR.cpp:29-30)."""
+
+    def __init__(self, mechanism="H2_Li", device=None):
+        self.lib = L.load()
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = device
+        h = ctypes.c_void_p()
+        st = self.lib.hf_init(mechanism.encode() if mechanism else None, int(device), ctypes.byref(h))
+        if st != L.HF_OK:
+            raise HyperFlowError(st, "hf_init(%r) failed" % mechanism)
+        self.h = h
+        self.ns = self.lib.hf_nspecies(h)
+        self.nv = self.ns + 3
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st, what=""):
+        if st == L.HF_OK:
+            return
+        msg = (self.lib.hf_last_error(self.h) or b"").decode()
+        cls = DomainError if st in (L.HF_ERR_INADMISSIBLE, L.HF_ERR_NEGATIVE, L.HF_ERR_FACE,
+                                    L.HF_ERR_COMBINE) else HyperFlowError
+        raise cls(st, (what + ": " if what else "") + msg)
+
+    def counters(self):
+        c = L.Counters()
+        self.lib.hf_get_counters(self.h, ctypes.byref(c))
+        return {f: getattr(c, f) for f, _ in L.Counters._fields_}
+
+    def set_timing(self, enable=True):
+        """Per-kernel-class CUDA-event timing (resets the sums)."""
+        self.lib.hf_set_timing(self.h, int(bool(enable)))
+
+    def timing(self):
+        """{"flux"|"chem"|"other": (ms, launches)} since set_timing(True)."""
+        ms = (ctypes.c_double * 3)()
+        n = (ctypes.c_int64 * 3)()
+        self.lib.hf_get_timing(self.h, ms, n)
+        return {k: (ms[i], n[i]) for i, k in enumerate(("flux", "chem", "other"))}
+
+    def set_rate_scale(self, scale=None):
+        if scale is None:
+            self.check(self.lib.hf_set_rate_scale(self.h, None))
+        else:
+            arr = (ctypes.c_double * 21)(*[float(s) for s in scale])
+            self.check(self.lib.hf_set_rate_scale(self.h, arr))
+
+
+# ------------------------------------------------------------------ physics.cpp
+def properties(ctx, q):
+    """Batched properties(): q (NV, count) -> (p, a, T, status); status 1 = inadmissible."""
+    _need_cuda64(q, "q")
+    q = q.contiguous()
+    n = q.shape[1]
+    p, a, T = (torch.empty(n, dtype=torch.float64, device=q.device) for _ in range(3))
+    st = torch.empty(n, dtype=torch.int32, device=q.device)
+    r = ctx.lib.hf_properties(ctx.h, _ptr(q), n, n, _ptr(p), _ptr(a), _ptr(T), _ptr(st), _stream())
+    if r not in (L.HF_OK, L.HF_ERR_INADMISSIBLE):
+        ctx.check(r, "properties")
+    return p, a, T, st
+
+
+def admissible(ctx, q):
+    """admissible() (physics.cpp:45-48) for each column of q."""
+    return properties(ctx, q)[3] == 0
+
+
+def hllc(ctx, left, right, props_l, props_r, direction):
+    """hllc() (physics.cpp:17-38): left/right (NV, n), props (3, n) = (p, a, T); direction 0=x, 1=y."""
+    for t, nm in ((left, "left"), (right, "right"), (props_l, "props_l"), (props_r, "props_r")):
+        _need_cuda64(t, nm)
+    n = left.shape[1]
+    left, right = left.contiguous(), right.contiguous()
+    props_l, props_r = props_l.contiguous(), props_r.contiguous()
+    out = torch.empty_like(left)
+    ctx.check(ctx.lib.hf_hllc(ctx.h, _ptr(left), _ptr(right), _ptr(props_l), _ptr(props_r), n, n, int(direction),
+                              _ptr(out), _stream()), "hllc")
+    return out
+
+
+# ------------------------------------------------------------------ grids
+def make_level(nx, ny, dx, dy, xlo=0.0, ylo=0.0, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+               boundary_hi=("transmissive", "reflecting"), inlet=None, wedge_start=0.0):
+    """hf_level from the reference's case keys (BlockAMR.cpp:38-59 defaults)."""
+    lv = L.Level()
+    lv.nx, lv.ny, lv.dx, lv.dy, lv.xlo, lv.ylo = int(nx), int(ny), float(dx), float(dy), float(xlo), float(ylo)
+    for d in range(2):
+        lv.periodic[d] = int(periodic[d])
+        lo, hi = boundary_lo[d], boundary_hi[d]
+        lv.bc_lo[d] = BC[lo] if isinstance(lo, str) else int(lo)
+        lv.bc_hi[d] = BC[hi] if isinstance(hi, str) else int(hi)
+    if inlet is not None:
+        for n, v in enumerate(inlet):
+            lv.inlet[n] = float(v)
+    lv.wedge_start = float(wedge_start)
+    return lv
+
+
+class PatchArray:
+    """One patch with ng ghost layers: a (NV, ny+2ng, pitch) float64 CUDA tensor."""
+
+    def __init__(self, nv, nx, ny, ng=2, ilo=0, jlo=0, device="cuda", pitch=None):
+        self.nv, self.nx, self.ny, self.ng = nv, nx, ny, ng
+        self.pitch = pitch or ((nx + 2 * ng + 1) // 2 * 2)
+        self.rows = ny + 2 * ng
+        self.data = torch.zeros(nv, self.rows, self.pitch, dtype=torch.float64, device=device)
+        p = L.Patch()
+        p.ilo, p.jlo, p.nx, p.ny, p.ng = ilo, jlo, nx, ny, ng
+        p.pitch, p.comp_stride, p.offset = self.pitch, self.rows * self.pitch, 0
+        self.patch = p
+
+    def interior(self):
+        g = self.ng
+        return self.data[:, g:g + self.ny, g:g + self.nx]
+
+    def ghosted(self):
+        """(NV, ny+2ng, nx+2ng) view including ghosts."""
+        return self.data[:, :, :self.nx + 2 * self.ng]
+
+    def like(self):
+        o = PatchArray(self.nv, self.nx, self.ny, self.ng, self.patch.ilo, self.patch.jlo, self.data.device,
+                       self.pitch)
+        return o
+
+
+def fill(ctx, level, patch_array):
+    """Ghost fill of a one-patch level (BlockAMR::fill + FlowBoundary)."""
+    ctx.check(ctx.lib.hf_fill_ghosts(ctx.h, ctypes.byref(level), ctypes.byref(patch_array.patch), 1,
+                                     _ptr(patch_array.data), _stream()), "fill")
+
+
+def euler_stage(ctx, level, u_in, u_out, h, first_order=False, u_old=None, form=L.HF_FLUX_PLAIN, faces=False):
+    """One Euler stage (BlockAMR.cpp:210-243) of a one-patch level; Heun combine with u_old.
+
+    Returns (fx, fy) face fluxes when faces=True (plain form only)."""
+    fx = fy = None
+    if faces:
+        nv, nx, ny = u_in.nv, u_in.nx, u_in.ny
+        fx = torch.empty(nv, ny, nx + 1, dtype=torch.float64, device=u_in.data.device)
+        fy = torch.empty(nv, ny + 1, nx, dtype=torch.float64, device=u_in.data.device)
+    bad = ctypes.c_int64(-1)
+    st = ctx.lib.hf_flux_update(ctx.h, ctypes.byref(level), ctypes.byref(u_in.patch), 1, _ptr(u_in.data),
+                                _ptr(u_old.data) if u_old is not None else None, _ptr(u_out.data), _ptr(fx),
+                                _ptr(fy), float(h), int(first_order), int(form), ctypes.byref(bad), _stream())
+    ctx.check(st, "euler stage (bad cell %d)" % bad.value)
+    return fx, fy
+
+
+def cfl_dt(ctx, level, patch_array, cfl):
+    """stableDt (BlockAMR.cpp:335-346)."""
+    dt = ctypes.c_double(0.0)
+    ctx.check(ctx.lib.hf_cfl_dt(ctx.h, ctypes.byref(level), ctypes.byref(patch_array.patch), 1,
+                                _ptr(patch_array.data), float(cfl), ctypes.byref(dt), _stream()), "cfl_dt")
+    return dt.value
+
+
+def validate(ctx, level, patch_array):
+    bad = ctypes.c_int64(-1)
+    ctx.check(ctx.lib.hf_validate(ctx.h, ctypes.byref(level), ctypes.byref(patch_array.patch), 1,
+                                  _ptr(patch_array.data), ctypes.byref(bad), _stream()), "validate")
+
+
+class ConservativeInterp:
+    """ConservativeInterp::interp (src/ConservativeInterp.cpp:18-51), ratio 2."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    def interp(self, coarse, fine, region):
+        """Fill fine cells of region (filo, fjlo, fihi, fjhi; fine level index) from coarse."""
+        r = (ctypes.c_int32 * 4)(*[int(v) for v in region])
+        self.ctx.check(self.ctx.lib.hf_interp_coarse_to_fine(self.ctx.h, ctypes.byref(coarse.patch),
+                                                             _ptr(coarse.data), ctypes.byref(fine.patch),
+                                                             _ptr(fine.data), r, _stream()), "interp")
+
+
+# ------------------------------------------------------------------ chemistry
+class ChemistryBatch:
+    """ChemistryBatch (src/chemistry_batch.hpp): all-or-nothing advance of a batch of cells.
+
+    form: "plain" (one thread per cell) or "persistent" (device work queue)."""
+
+    def __init__(self, ctx, form="persistent", rtol=1e-8, atol=1e-15):
+        self.ctx = ctx
+        self.form = {"plain": L.HF_CHEM_PLAIN, "persistent": L.HF_CHEM_PERSISTENT}[form]
+        self.rtol, self.atol = rtol, atol
+
+    def advance(self, field, dt, count=None, dt_cell=None, cell_index=None, comp_stride=None):
+        """field: (NV, n) float64 CUDA tensor (SoA), advanced in place over dt.
+
+        Raises RuntimeError("chemistry cell k: ...") on failure; field is unchanged then."""
+        _need_cuda64(field, "field")
+        if cell_index is None:
+            if not field.is_contiguous():
+                raise ValueError("field must be contiguous (NV, n)")
+            n = field.shape[1] if count is None else int(count)
+            if n > field.shape[1]:
+                raise ValueError("invalid chemistry batch extent")
+            cs = field.shape[1]
+        else:
+            n = cell_index.numel() if count is None else int(count)
+            cs = int(comp_stride)
+        dtc = None
+        if dt_cell is not None:
+            _need_cuda64(dt_cell, "dt_cell")
+        first = ctypes.c_int64(-1)
+        st = self.ctx.lib.hf_chem_advance(self.ctx.h, _ptr(field), cs, _ptr(cell_index), n, float(dt),
+                                          _ptr(dt_cell), float(self.rtol), float(self.atol), self.form,
+                                          ctypes.byref(first), _stream())
+        if st in (L.HF_ERR_CHEM_FAIL, L.HF_ERR_MAXSTEPS):
+            e = RuntimeError("chemistry cell %d: %s" % (first.value,
+                                                        (self.ctx.lib.hf_last_error(self.ctx.h) or b"").decode()))
+            e.first_failed = first.value
+            e.status = st
+            raise e
+        self.ctx.check(st, "chemistry")
+        return field
+
+
+# ------------------------------------------------------------------ stepper
+class Stepper:
+    """Strang-split reacting-Euler stepper on a uniform one-patch level.
+
+    step(): flow(dt/2); react(dt); flow(dt/2) with rollback and dt halving
+    (BlockAMR.cpp:409-419).  U0: (NV, ny, nx) float64 CUDA tensor."""
+
+    def __init__(self, ctx, level, U0, chemistry=True, rtol=1e-8, atol=1e-15, flux="fused", chem="persistent"):
+        _need_cuda64(U0, "U0")
+        self.ctx = ctx
+        self.level = level
+        self.nv, self.ny, self.nx = U0.shape
+        U0 = U0.contiguous()
+        h = ctypes.c_void_p()
+        ff = {"plain": L.HF_FLUX_PLAIN, "fused": L.HF_FLUX_FUSED}[flux]
+        cf = {"plain": L.HF_CHEM_PLAIN, "persistent": L.HF_CHEM_PERSISTENT}[chem]
+        torch.cuda.synchronize()
+        ctx.check(ctx.lib.hf_stepper_create(ctx.h, ctypes.byref(level), _ptr(U0), int(bool(chemistry)), float(rtol),
+                                            float(atol), ff, cf, ctypes.byref(h)), "stepper_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.hf_stepper_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt=0.0, cfl=0.5):
+        d = ctypes.c_double(float(dt))
+        self.ctx.check(self.ctx.lib.hf_stepper_step(self.h, float(cfl), ctypes.byref(d), _stream()), "step")
+        return d.value
+
+    def state(self):
+        out = torch.empty(self.nv, self.ny, self.nx, dtype=torch.float64, device="cuda")
+        self.ctx.check(self.ctx.lib.hf_stepper_get(self.h, _ptr(out), _stream()), "stepper_get")
+        return out
+
+    def set_host(self, U):
+        """Copy valid cells in from host memory (torch CPU tensor, (NV, ny, nx))."""
+        self.ctx.check(self.ctx.lib.hf_stepper_set_host(self.h, ctypes.c_void_p(U.data_ptr()), _stream()), "set_host")
+
+    def get_host(self, U):
+        self.ctx.check(self.ctx.lib.hf_stepper_get_host(self.h, ctypes.c_void_p(U.data_ptr()), _stream()), "get_host")
+        return U
+
+    @property
+    def time(self):
+        return self.ctx.lib.hf_stepper_time(self.h)

@@ -1,0 +1,85 @@
+"""Seeded synthetic workloads (initial conditions) of the benchmark configurations.
+
+  det1d  : planar detonation, 2000 x 2 cells on 0.1 m (dx = 5e-5 m), H2/O2 with 70% (mole)
+           diluent at 1 atm / 298 K, a 20-cell driver at 40 atm / 3000 K; reflecting left,
+           transmissive right, reflecting top/bottom (the sun_cj case layout).
+  det2d  : cellular detonation, 2048 x 512 cells, dx = 1e-4 m (0.2048 m x 0.0512 m),
+           same mixture, a 64-column hot band at 40 atm / 3000 K, density perturbed by a
+           seeded U(-1%, +1%) in those columns; periodic in y, reflecting left, transmissive
+           right.
+  chem   : 2^20 independent cells, T ~ U[800, 2500] K, p ~ logU[0.1, 10] atm,
+           phi ~ logU[0.3, 3], diluent ~ U[0, 0.8], dt ~ logU[1e-7, 1e-6] s.
+The diluent is argon (the inert AR extension species, 10-species mechanism) unless
+diluent="N2" is asked for (9 species, the reference mechanism as is).
+"""
+import numpy as np
+
+from . import mechanism as M
+
+
+def _ns(diluent):
+    return 10 if diluent.upper() == "AR" else 9
+
+
+def detonation(nx, ny, dx, hot_columns, seed=0, diluent="AR", dilution=0.7, T0=298.0, p0=101325.0, T_hot=3000.0,
+               p_hot=40 * 101325.0, perturb=0.01):
+    """(NV, ny, nx) initial state: fresh mixture with a hot band in the first columns."""
+    ns = _ns(diluent)
+    X = M.mixture_X(1.0, dilution, "AR" if ns == 10 else "N2", ns)
+    fresh = M.primitive(T0, p0, X=X, ns=ns)
+    hot = M.primitive(T_hot, p_hot, X=X, ns=ns)
+    U = np.empty((ns + 3, ny, nx))
+    U[:] = fresh[:, None, None]
+    U[:, :, :hot_columns] = hot[:, None, None]
+    if perturb:
+        rng = np.random.default_rng(seed)
+        f = 1.0 + rng.uniform(-perturb, perturb, size=(ny, hot_columns))
+        U[:, :, :hot_columns] *= f[None]
+    return U, fresh
+
+
+def det2d(seed=0, diluent="AR", nx=2048, ny=512, hot_columns=64):
+    U, fresh = detonation(nx, ny, 1e-4, hot_columns=min(hot_columns, nx), seed=seed, diluent=diluent)
+    level = dict(nx=nx, ny=ny, dx=1e-4, dy=1e-4, periodic=(0, 1), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("transmissive", "reflecting"), inlet=fresh)
+    return U, level
+
+
+def det1d(diluent="AR", nx=2000):
+    U, fresh = detonation(nx, 2, 0.1 / nx, hot_columns=20, perturb=0.0, diluent=diluent)
+    level = dict(nx=nx, ny=2, dx=0.1 / nx, dy=0.1 / nx, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("transmissive", "reflecting"), inlet=fresh)
+    return U, level
+
+
+def chem_batch(n=1 << 20, seed=0, diluent="AR"):
+    """(NV, n) states and (n,) intervals of independent 0D cells."""
+    ns = _ns(diluent)
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(800.0, 2500.0, n)
+    p = 101325.0 * np.exp(rng.uniform(np.log(0.1), np.log(10.0), n))
+    phi = np.exp(rng.uniform(np.log(0.3), np.log(3.0), n))
+    dil = rng.uniform(0.0, 0.8, n)
+    dt = np.exp(rng.uniform(np.log(1e-7), np.log(1e-6), n))
+    W = M.MW[:ns]
+    dsp = M.SPECIES.index("AR" if ns == 10 else "N2")
+    X = np.zeros((n, ns))
+    X[:, 0] = 2.0 * phi
+    X[:, 1] = 1.0
+    X[:, :2] *= ((1.0 - dil) / X[:, :2].sum(1))[:, None]
+    X[:, dsp] += dil
+    if ns == 9:
+        # air-like nitrogen when the diluent is nitrogen: keep at least 3.76 N2 per O2 mole
+        pass
+    Y = X * W / (X * W).sum(1, keepdims=True)
+    rho = p / (M.GAS_CONSTANT * T * (Y / W).sum(1))
+    e = np.empty(n)
+    lo, hi = M.NASA_LOW[:ns], M.NASA_HIGH[:ns]
+    for sel, a in ((T <= 1000.0, lo), (T > 1000.0, hi)):
+        t = T[sel][:, None]
+        hRT = a[:, 0] + t * (a[:, 1] / 2 + t * (a[:, 2] / 3 + t * (a[:, 3] / 4 + t * a[:, 4] / 5))) + a[:, 5] / t
+        e[sel] = M.GAS_CONSTANT * T[sel] * ((Y[sel] / W) * (hRT - 1.0)).sum(1)
+    U = np.zeros((ns + 3, n))
+    U[:ns] = (rho[:, None] * Y).T
+    U[ns + 2] = rho * e
+    return U, dt

@@ -1,0 +1,206 @@
+/* hyperflow_gpu.h - C ABI of the GB300 reacting-Euler step (HyperFlow V3 hot path).
+ *
+ * The reference has no C ABI: its time stepper (BlockAMR, HyperFlow_V3/src/BlockAMR.cpp)
+ * calls C++ functions per block.  Each entry point below replaces one of them and
+ * keeps its argument meaning and its error behaviour, with return codes in place of
+ * exceptions.  Conventions:
+ *   - A cell state is NV = NS+3 doubles: rhoY_0..rhoY_{NS-1}, rho*u, rho*v, rho*E
+ *     (HyperFlow_V3/src/solver.hpp:17-25).  NS = 9 for H2_Li.yaml; NS = 10 with the
+ *     inert AR extension species.
+ *   - Grid data is structure-of-arrays FP64 in caller-owned DEVICE memory: component n
+ *     of cell (i, j) of a patch lives at base[offset + n*comp_stride + (j+ng)*pitch + (i+ng)],
+ *     i in [-ng, nx+ng), j in [-ng, ny+ng) (valid cells plus ng ghost layers).
+ *   - Batches of cells (chemistry, properties) are SoA with a component stride.
+ *   - Every call is stream-ordered on the caller's cudaStream_t (passed as void*; NULL =
+ *     legacy default stream).  Calls that report a status synchronise that stream.
+ *   - Device code never traps; failures are flags the host reads after the stream syncs.
+ *   - One hf_ctx per host thread; a context is not re-entrant (chemistry_batch.hpp:6-7).
+ */
+#ifndef HYPERFLOW_GPU_H
+#define HYPERFLOW_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HF_EXPORT __attribute__((visibility("default")))
+#else
+#define HF_EXPORT
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hf_status {
+    HF_OK = 0,
+    HF_ERR_INADMISSIBLE = 1, /* std::domain_error of properties()/validate() (physics.cpp:8,13) */
+    HF_ERR_CHEM_FAIL = 2,    /* a chemistry cell failed (chemistry_batch.cpp:40-49); see first_failed */
+    HF_ERR_MAXSTEPS = 3,     /* chemistry step limit reached (CVodeSetMaxNumSteps(5000), chemistry.cpp:25) */
+    HF_ERR_ARG = 4,          /* std::invalid_argument */
+    HF_ERR_CUDA = 5,         /* a CUDA runtime call failed */
+    HF_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+    HF_ERR_NEGATIVE = 7,     /* materially negative species after a stage (BlockAMR.cpp:320-321) */
+    HF_ERR_FACE = 8,         /* a face fell back to an inadmissible cell state: properties() throws
+                                inside the flux loop (BlockAMR.cpp:223), which only run()'s
+                                rollback catches */
+    HF_ERR_COMBINE = 9       /* the Heun combination is inadmissible (validate, BlockAMR.cpp:269) */
+} hf_status;
+
+/* Boundary kinds: the strings of the reference's case JSON (BlockAMR.cpp:38-59). */
+enum { HF_BC_REFLECTING = 0, HF_BC_TRANSMISSIVE = 1, HF_BC_INFLOW = 2, HF_BC_WEDGE = 3 };
+
+/* Chemistry forms. */
+enum { HF_CHEM_PLAIN = 0,      /* one thread per cell, one launch (the drop-in form) */
+       HF_CHEM_PERSISTENT = 1  /* persistent launch pulling cells from a device work queue */ };
+
+/* Flux forms. */
+enum { HF_FLUX_PLAIN = 0,      /* face kernels + update kernel, one launch set per patch; needs
+                                  filled ghosts (hf_fill_ghosts) */
+       HF_FLUX_FUSED = 1       /* one fused kernel per level: TMA tile + halo in shared memory,
+                                  domain boundaries resolved while loading (no ghost fill needed
+                                  for a level made of one patch that covers the domain) */ };
+
+typedef struct hf_ctx hf_ctx;
+
+/* A level: the domain box at this level and its boundary description
+ * (BlockAMR.cpp:48-59; FlowBoundary.hpp:8-11; geometry of BlockAMR.cpp:211,225). */
+typedef struct hf_level {
+    int32_t nx, ny;            /* domain cells at this level; domain small end is (0,0) */
+    double dx, dy;             /* cell size */
+    double xlo, ylo;           /* ProbLo */
+    int32_t periodic[2];
+    int32_t bc_lo[2], bc_hi[2];/* HF_BC_* per direction; WEDGE only for bc_lo[1] */
+    double inlet[13];          /* fixed inflow state ("fresh"), first NV entries used */
+    double wedge_start;        /* x of the wedge tip (bc_lo[1] == HF_BC_WEDGE) */
+} hf_level;
+
+/* A patch (an AMReX box of the level) inside a level buffer. */
+typedef struct hf_patch {
+    int32_t ilo, jlo;          /* level index of the first valid cell */
+    int32_t nx, ny;            /* valid cells */
+    int32_t ng;                /* ghost layers stored (>= 2) */
+    int32_t pad_;
+    int64_t pitch;             /* elements between rows, >= nx + 2 ng (even for HF_FLUX_FUSED) */
+    int64_t comp_stride;       /* elements between components, >= pitch*(ny+2 ng) (even for FUSED) */
+    int64_t offset;            /* element offset of this patch's storage in the level buffer */
+} hf_patch;
+
+/* Counters kept by a context (BlockAMR.cpp:426-438 summary fields). */
+typedef struct hf_counters {
+    int64_t first_order_stages;   /* positivity_first_order_stages */
+    int64_t roundoff_repairs;     /* roundoff_redistributions */
+    int64_t retries;              /* retries (host stepper) */
+    int64_t chem_cell_calls;      /* chemistry_cell_calls */
+    int64_t chem_steps;           /* accepted + rejected integrator steps */
+    int64_t kernel_launches;      /* kernels launched by this context */
+} hf_counters;
+
+/* ---- context (replaces Cantera::newSolution(mechanism) + ChemistryBatch construction,
+ *      BlockAMR.cpp:29-30, chemistry_batch.cpp:9-20) ---- */
+/* mechanism: NULL, "H2_Li", a path ending in "H2_Li.yaml" (9 species), or "H2_Li+AR"
+ * (10 species, inert AR extension).  device: CUDA ordinal. */
+HF_EXPORT hf_status hf_init(const char* mechanism, int device, hf_ctx** out);
+HF_EXPORT void hf_destroy(hf_ctx* ctx);
+HF_EXPORT int hf_nspecies(const hf_ctx* ctx);
+HF_EXPORT const char* hf_last_error(const hf_ctx* ctx);
+HF_EXPORT void hf_get_counters(const hf_ctx* ctx, hf_counters* out);
+/* Device time per kernel class, measured with CUDA events recorded on the caller's stream
+ * around each launch while enabled (enable != 0 also resets the sums): ms[0] flux stages
+ * (hf_flux_update), ms[1] chemistry (hf_chem_advance), ms[2] ghost fill and reductions.
+ * launches[k] counts the launches of each class.  Extension: the reference keeps host wall
+ * timers only (flow_seconds / chemistry_seconds, BlockAMR.cpp:267-284,435). */
+HF_EXPORT void hf_set_timing(hf_ctx* ctx, int enable);
+HF_EXPORT void hf_get_timing(const hf_ctx* ctx, double ms[3], int64_t launches[3]);
+/* Multiply each reaction's pre-exponential factor(s) by scale[r] (21 entries; NULL resets).
+ * Used for d/d ln A_k sensitivity checks; not in the reference. */
+HF_EXPORT hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale);
+
+/* ---- EOS / flux primitives on batches (physics.cpp:4-48) ---- */
+/* properties(): q is SoA [NV][stride] device memory with count cells; writes p, a, T and
+ * status[i] (0 ok, 1 inadmissible).  Returns HF_OK or HF_ERR_INADMISSIBLE if any failed. */
+HF_EXPORT hf_status hf_properties(hf_ctx* ctx, const double* q, int64_t stride, int64_t count, double* p,
+                        double* a, double* T, int32_t* status, void* stream);
+/* hllc(): left/right SoA [NV][stride], dir 0 = x (n = mx), 1 = y (n = my); props_l/r are
+ * SoA [3][stride] (p, a, T).  flux SoA [NV][stride]. */
+HF_EXPORT hf_status hf_hllc(hf_ctx* ctx, const double* left, const double* right, const double* props_l,
+                  const double* props_r, int64_t stride, int64_t count, int dir, double* flux,
+                  void* stream);
+
+/* ---- ghost fill (BlockAMR::fill, FlowBoundary::operator(), BlockAMR.cpp:137-146,
+ *      FlowBoundary.hpp:12-36) on one level: same-level exchange (incl. periodic images),
+ *      then physical boundaries in AMReX order (faces, then corners). ---- */
+HF_EXPORT hf_status hf_fill_ghosts(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
+                         double* U, void* stream);
+
+/* ---- coarse -> fine interpolation (ConservativeInterp::interp, ConservativeInterp.cpp:18-51).
+ * For every coarse cell (ci, cj) of the coarse index box [cilo..cihi] x [cjlo..cjhi]
+ * (fine box coarsened), reads coarse cell and its 4 neighbours from the coarse patch and
+ * writes the children that fall inside the fine target region [filo..fihi] x [fjlo..fjhi]
+ * (fine level index) of the fine patch. ---- */
+HF_EXPORT hf_status hf_interp_coarse_to_fine(hf_ctx* ctx, const hf_patch* coarse, const double* Uc,
+                                   const hf_patch* fine, double* Uf, const int32_t region[4],
+                                   void* stream);
+
+/* ---- one Euler stage of one level (BlockAMR::euler body, BlockAMR.cpp:210-243) plus the
+ * Heun combine of BlockAMR::flow (BlockAMR.cpp:268-269) when U_old is non-NULL:
+ *   U_out = [U_old + E(U_in)]/2  (U_old given)   or   U_out = E(U_in),
+ *   E(q) = q - h/dx (Fx(i+1)-Fx(i)) - h/dy (Fy(j+1)-Fy(j)).
+ * U_in must have filled ghosts for HF_FLUX_PLAIN.  fx/fy (nullable) receive face fluxes
+ * (x faces: [NV][ny][nx+1] per patch, y faces [NV][ny+1][nx]) for reflux.
+ * first_order: face states qb/qc (BlockAMR.cpp:220).  Each updated cell is validated
+ * (BlockAMR.cpp:257); returns HF_ERR_INADMISSIBLE (-> first-order redo) when a stage
+ * output is inadmissible, HF_ERR_NEGATIVE when a species went negative by more than
+ * roundoff (also -> first-order redo), HF_ERR_FACE or HF_ERR_COMBINE (-> rollback), and
+ * repairs roundoff-negative species like repairRoundoff (BlockAMR.cpp:299-334).
+ * HF_FLUX_FUSED requires npatch == 1, a patch covering the level domain, ng even, and
+ * fx == fy == NULL.
+ * bad_cell (nullable) receives the lowest failing linear cell index or -1. ---- */
+HF_EXPORT hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
+                         const double* U_in, const double* U_old, double* U_out, double* fx,
+                         double* fy, double h, int first_order, int form, int64_t* bad_cell,
+                         void* stream);
+
+/* ---- chemistry (ChemistryBatch::advance, chemistry_batch.cpp:21-50 over
+ * Chemistry::advance, chemistry.cpp:55-76).  U is SoA [NV][stride] device memory holding
+ * count cells (or a level buffer when cell_index is given: cell_index[i] is the element
+ * index of cell i's component 0, components comp_stride apart).  dt: one interval for all,
+ * or dt_cell[i] per cell when dt_cell is non-NULL (extension).  rtol/atol: 1e-8/1e-15 in
+ * the reference.  All-or-nothing: on failure U is unchanged and *first_failed is the lowest
+ * failing cell index.  form: HF_CHEM_PLAIN or HF_CHEM_PERSISTENT. ---- */
+HF_EXPORT hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index,
+                          int64_t count, double dt, const double* dt_cell, double rtol, double atol,
+                          int form, int64_t* first_failed, void* stream);
+
+/* ---- reductions ---- */
+/* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the valid cells of the patches:
+ * *dt = cfl / max((|u|+a)/dx + (|v|+a)/dy).  HF_ERR_INADMISSIBLE if a cell is not. */
+HF_EXPORT hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
+                    const double* U, double cfl, double* dt, void* stream);
+/* BlockAMR::validate (BlockAMR.cpp:286-298): HF_ERR_INADMISSIBLE and the lowest failing
+ * linear cell index if any valid cell is inadmissible. */
+HF_EXPORT hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
+                      const double* U, int64_t* bad_cell, void* stream);
+
+/* ---- host stepper over a single-patch uniform level (BlockAMR::run loop body,
+ * BlockAMR.cpp:409-419): Strang flow(dt/2), react(dt), flow(dt/2), each flow a Heun pair
+ * of Euler stages; rollback and dt halving up to 18 attempts. ---- */
+typedef struct hf_stepper hf_stepper;
+/* U0: initial valid cells, SoA [NV][ny][nx] in DEVICE memory (copied in). */
+HF_EXPORT hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0, int chemistry,
+                            double rtol, double atol, int flux_form, int chem_form,
+                            hf_stepper** out);
+HF_EXPORT void hf_stepper_destroy(hf_stepper* st);
+/* One Strang step.  *dt in: requested interval (<= 0: CFL dt with the given cfl);
+ * out: the accepted interval. */
+HF_EXPORT hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream);
+/* Copy the valid cells out, SoA [NV][ny][nx], to DEVICE memory. */
+HF_EXPORT hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream);
+/* Copy valid cells in from / out to HOST memory (pinned or pageable), SoA [NV][ny][nx]. */
+HF_EXPORT hf_status hf_stepper_set_host(hf_stepper* st, const double* U, void* stream);
+HF_EXPORT hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream);
+HF_EXPORT double hf_stepper_time(const hf_stepper* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,296 @@
+"""ctypes wrapper around the CPU oracle (``liboracle.so``).
+
+Test infrastructure only: the tests, ``__graft_entry__.smoke()`` and the CPU
+baseline leg of ``bench.py`` use it as the checker.  The GPU package never
+imports it.  States are AoS float64 arrays of shape (..., NS+3) in the
+reference's component order (rhoY_0..rhoY_{NS-1}, rho*u, rho*v, rho*E).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+BC_REFLECTING, BC_TRANSMISSIVE, BC_INFLOW, BC_WEDGE = 0, 1, 2, 3
+MAXV = 13
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("xlo", ctypes.c_double), ("ylo", ctypes.c_double),
+                ("periodic", ctypes.c_int * 2), ("bc_lo", ctypes.c_int * 2), ("bc_hi", ctypes.c_int * 2),
+                ("inlet", ctypes.c_double * MAXV), ("wedge_start", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("first_order_stages", ctypes.c_long), ("roundoff_repairs", ctypes.c_long),
+                ("retries", ctypes.c_long), ("chem_failures", ctypes.c_long)]
+
+
+def build():
+    """Compile liboracle.so with the committed Makefile (g++ only)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.or_set_species.argtypes = [ctypes.c_int]
+        L.or_molecular_weight.restype = ctypes.c_double
+        L.or_mix_e.restype = ctypes.c_double
+        L.or_mix_e.argtypes = [_dp, ctypes.c_double]
+        L.or_mix_cv.restype = ctypes.c_double
+        L.or_mix_cv.argtypes = [_dp, ctypes.c_double]
+        L.or_species_thermo.argtypes = [ctypes.c_double, _dp, _dp, _dp]
+        L.or_properties.argtypes = [_dp, ctypes.c_int64, _dp, _dp, _dp, _ip]
+        L.or_hllc.argtypes = [_dp, _dp, ctypes.c_int, _dp, _dp, _dp]
+        L.or_minmod.argtypes = [_dp, _dp, _dp, ctypes.c_int]
+        L.or_net_production.argtypes = [ctypes.c_double, _dp, _dp]
+        L.or_progress.argtypes = [ctypes.c_double, _dp, _dp, _dp, _dp, _dp]
+        L.or_chem_rhs.argtypes = [ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+        L.or_chem_jac.argtypes = [ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, ctypes.c_int]
+        L.or_chem_advance.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_long, _lp]
+        L.or_chem_batch.restype = ctypes.c_int64
+        L.or_chem_batch.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int, _lp]
+        L.or_rodas4_circle.argtypes = [_dp, ctypes.c_double, ctypes.c_int]
+        L.or_fill_ghosts.argtypes = [ctypes.POINTER(Grid), _dp]
+        L.or_euler_stage.argtypes = [ctypes.POINTER(Grid), _dp, _dp, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.or_repair_roundoff.argtypes = [ctypes.POINTER(Grid), _dp, _lp]
+        L.or_validate.argtypes = [ctypes.POINTER(Grid), _dp]
+        L.or_flow.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_double, ctypes.POINTER(Stats)]
+        L.or_react.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.or_cfl_dt.restype = ctypes.c_double
+        L.or_cfl_dt.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_double]
+        L.or_strang_step.argtypes = [ctypes.POINTER(Grid), _dp, _dp, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_int, ctypes.POINTER(Stats)]
+        L.or_interp_cell.restype = ctypes.c_double
+        L.or_interp_cell.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+def set_species(ns):
+    if lib().or_set_species(ns) != 0:
+        raise ValueError("species count must be 9 or 10")
+
+
+def nspecies():
+    return lib().or_nspecies()
+
+
+def molecular_weights():
+    return np.array([lib().or_molecular_weight(k) for k in range(nspecies())])
+
+
+def species_thermo(T):
+    ns = nspecies()
+    cp, h, s = np.zeros(ns), np.zeros(ns), np.zeros(ns)
+    lib().or_species_thermo(float(T), _p(cp), _p(h), _p(s))
+    return cp, h, s
+
+
+def mix_e(Y, T):
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    return lib().or_mix_e(_p(Y), float(T))
+
+
+def mix_cv(Y, T):
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    return lib().or_mix_cv(_p(Y), float(T))
+
+
+def properties(q):
+    """Batched physics.cpp:4-15; returns (p, a, T, status) with status 1 = inadmissible."""
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, nspecies() + 3)
+    n = len(q)
+    p, a, T = np.zeros(n), np.zeros(n), np.zeros(n)
+    st = np.zeros(n, dtype=np.int32)
+    lib().or_properties(_p(q), n, _p(p), _p(a), _p(T), st.ctypes.data_as(_ip))
+    return p, a, T, st
+
+
+def hllc(l, r, n, pl, pr):
+    l = np.ascontiguousarray(l, dtype=np.float64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    pl = np.ascontiguousarray(pl, dtype=np.float64)
+    pr = np.ascontiguousarray(pr, dtype=np.float64)
+    out = np.zeros(nspecies() + 3)
+    lib().or_hllc(_p(l), _p(r), int(n), _p(pl), _p(pr), _p(out))
+    return out
+
+
+def minmod(a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.zeros_like(a)
+    lib().or_minmod(_p(a), _p(b), _p(out), a.size)
+    return out
+
+
+def net_production(T, C):
+    C = np.ascontiguousarray(C, dtype=np.float64)
+    w = np.zeros(nspecies())
+    lib().or_net_production(float(T), _p(C), _p(w))
+    return w
+
+
+def progress(T, C):
+    C = np.ascontiguousarray(C, dtype=np.float64)
+    kf, kr, qf, qr = (np.zeros(21) for _ in range(4))
+    lib().or_progress(float(T), _p(C), _p(kf), _p(kr), _p(qf), _p(qr))
+    return kf, kr, qf, qr
+
+
+def chem_rhs(rho, e, y, T_guess=1000.0):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    T = np.array([T_guess])
+    dy = np.zeros(nspecies() - 1)
+    st = lib().or_chem_rhs(float(rho), float(e), _p(y), _p(T), _p(dy))
+    return dy, float(T[0]), st
+
+
+def chem_jac(rho, e, y, T_guess=1000.0, fd=False):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    T = np.array([T_guess])
+    n = nspecies() - 1
+    J = np.zeros(n * n)
+    st = lib().or_chem_jac(float(rho), float(e), _p(y), _p(T), _p(J), int(fd))
+    return J.reshape(n, n), st
+
+
+def chem_advance(u, dt, rtol=1e-8, atol=1e-15, max_steps=5000):
+    """One cell through chemistry.cpp:55-76; returns (new state, status, attempts)."""
+    u = np.array(u, dtype=np.float64)
+    steps = ctypes.c_long(0)
+    st = lib().or_chem_advance(_p(u), float(dt), float(rtol), float(atol), int(max_steps), ctypes.byref(steps))
+    return u, st, steps.value
+
+
+def chem_batch(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
+    """chemistry_batch.cpp:21-50 over AoS cells; returns (U_new, first_failed or -1, attempts)."""
+    U = np.ascontiguousarray(np.array(U, dtype=np.float64).reshape(-1, nspecies() + 3))
+    steps = np.zeros(len(U), dtype=np.int64)
+    dtc = None if dt_cell is None else np.ascontiguousarray(dt_cell, dtype=np.float64)
+    bad = lib().or_chem_batch(_p(U), len(U), float(dt), None if dtc is None else _p(dtc), float(rtol),
+                              float(atol), int(threads), steps.ctypes.data_as(_lp))
+    return U, int(bad), steps
+
+
+def rodas4_circle(y, tend, nsteps):
+    y = np.array(y, dtype=np.float64)
+    lib().or_rodas4_circle(_p(y), float(tend), int(nsteps))
+    return y
+
+
+def make_grid(nx, ny, dx, dy, xlo=0.0, ylo=0.0, periodic=(0, 0), bc_lo=(0, 0), bc_hi=(1, 0),
+              inlet=None, wedge_start=0.0):
+    g = Grid()
+    g.nx, g.ny, g.dx, g.dy, g.xlo, g.ylo = nx, ny, dx, dy, xlo, ylo
+    g.periodic[0], g.periodic[1] = periodic
+    g.bc_lo[0], g.bc_lo[1] = bc_lo
+    g.bc_hi[0], g.bc_hi[1] = bc_hi
+    if inlet is not None:
+        for n, v in enumerate(inlet):
+            g.inlet[n] = float(v)
+    g.wedge_start = wedge_start
+    return g
+
+
+def ghosted(interior):
+    """(ny, nx, nv) interior -> (ny+4, nx+4, nv) ghosted array (ghosts NaN)."""
+    ny, nx, nv = interior.shape
+    U = np.full((ny + 4, nx + 4, nv), np.nan)
+    U[2:-2, 2:-2] = interior
+    return U
+
+
+def fill_ghosts(g, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    lib().or_fill_ghosts(ctypes.byref(g), _p(U))
+    return U
+
+
+def euler_stage(g, Ug, h, first_order=False):
+    Ug = np.ascontiguousarray(Ug, dtype=np.float64)
+    out = Ug.copy()
+    nv = Ug.shape[-1]
+    fx = np.zeros((g.ny, g.nx + 1, nv))
+    fy = np.zeros((g.ny + 1, g.nx, nv))
+    st = lib().or_euler_stage(ctypes.byref(g), _p(Ug), _p(out), float(h), int(first_order), _p(fx), _p(fy))
+    return out, fx, fy, st
+
+
+def flow(g, U, h):
+    U = np.ascontiguousarray(U, dtype=np.float64).copy()
+    s = Stats()
+    st = lib().or_flow(ctypes.byref(g), _p(U), float(h), ctypes.byref(s))
+    return U, st, s
+
+
+def cfl_dt(g, U, cfl):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    return lib().or_cfl_dt(ctypes.byref(g), _p(U), float(cfl))
+
+
+def strang_step(g, U, dt, chemistry=True, rtol=1e-8, atol=1e-15, threads=0):
+    U = np.ascontiguousarray(U, dtype=np.float64).copy()
+    d = np.array([dt], dtype=np.float64)
+    s = Stats()
+    st = lib().or_strang_step(ctypes.byref(g), _p(U), _p(d), int(chemistry), float(rtol), float(atol),
+                              int(threads), ctypes.byref(s))
+    return U, float(d[0]), st, s
+
+
+def interp_cell(q, xm, xp, ym, yp):
+    args = [np.ascontiguousarray(v, dtype=np.float64) for v in (q, xm, xp, ym, yp)]
+    out = np.zeros((4, len(args[0])))
+    theta = lib().or_interp_cell(*[_p(a) for a in args], _p(out))
+    return out, theta
+
+
+SPECIES = ["H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2", "AR"]
+GAS_CONSTANT = 8314.46261815324
+
+
+def composition(spec, kind="X"):
+    """'H2:2,O2:1,N2:3.76' -> normalised vector over the active species."""
+    ns = nspecies()
+    v = np.zeros(ns)
+    for part in spec.split(","):
+        name, val = part.split(":")
+        v[SPECIES.index(name.strip())] = float(val)
+    return v / v.sum()
+
+
+def primitive(T, p, X=None, Y=None, u=0.0, v=0.0):
+    """BlockAMR.cpp:20-24 (state from T, p and mole or mass fractions), restated."""
+    W = molecular_weights()
+    if Y is None:
+        X = np.asarray(X, dtype=np.float64)
+        Y = X * W / np.sum(X * W)
+    Y = np.asarray(Y, dtype=np.float64)
+    rho = p / (GAS_CONSTANT * T * np.sum(Y / W))
+    e = mix_e(Y, T)
+    q = np.zeros(len(W) + 3)
+    q[:len(W)] = rho * Y
+    q[len(W)] = rho * u
+    q[len(W) + 1] = rho * v
+    q[len(W) + 2] = rho * (e + 0.5 * (u * u + v * v))
+    return q
