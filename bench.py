@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cfl", type=float, default=0.5)
+    p.add_argument("--flux", default="fused", choices=["fused", "plain"], help="flux form of the headline run")
+    p.add_argument("--chem", default="persistent", choices=["persistent", "plain"],
+                   help="chemistry form of the headline run")
     p.add_argument("--nx", type=int, default=NX)
     p.add_argument("--ny", type=int, default=NY)
     return p.parse_args()
@@ -209,7 +212,7 @@ def run_ours(args):
         return max_over_ranks(ms), ck, tm, {k: c1[k] - c0[k] for k in c1}
 
     clocks = Clocks(local)
-    ms, ck, tm, cnt = timed("fused", "persistent", args.steps, args.warmup, timing=True, clocks=clocks)
+    ms, ck, tm, cnt = timed(args.flux, args.chem, args.steps, args.warmup, timing=True, clocks=clocks)
     value = world * cells * args.steps / (ms * 1e-3)
     plain = None
     if not args.no_plain:
@@ -220,7 +223,7 @@ def run_ours(args):
 
     e2e = None
     if not args.no_e2e:
-        st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux="fused", chem="persistent")
+        st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=args.flux, chem=args.chem)
         host = torch.from_numpy(U0.copy()).pin_memory()
         for _ in range(args.warmup):
             st.set_host(host)

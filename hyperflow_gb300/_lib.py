@@ -41,6 +41,10 @@ class Counters(ctypes.Structure):
                 ("chem_cell_calls", _i64), ("chem_steps", _i64), ("kernel_launches", _i64)]
 
 
+class ChemHistory(ctypes.Structure):
+    _fields_ = [("h", _vp), ("cost", _vp)]
+
+
 # (name, restype, argtypes) for every entry point of the header
 SIGNATURES = [
     ("hf_init", _i32, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -59,6 +63,7 @@ SIGNATURES = [
     ("hf_flux_update", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _vp, _vp, _vp,
                               _vp, _d, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
+    ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
     ("hf_cfl_dt", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d, _dp, _vp]),
     ("hf_validate", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp,
                            ctypes.POINTER(_i64), _vp]),

@@ -4,6 +4,8 @@
 // codes (see the header for the mapping).
 #include <cuda.h>
 #include <cstdio>
+#include <climits>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -382,26 +384,38 @@ hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* pat
     return HF_OK;
 }
 
-hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index, int64_t count,
-                          double dt, const double* dt_cell, double rtol, double atol, int form, int64_t* first_failed,
-                          void* stream) {
+static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index, int64_t count,
+                             double dt, const double* dt_cell, double rtol, double atol, int form,
+                             const hf_chem_history* hist, int64_t* first_failed, void* stream) {
     if (first_failed) *first_failed = -1;
-    if (!ctx || !U || count < 0 || (!cell_index && comp_stride < count) || (!dt_cell && (!(dt > 0) || !std::isfinite(dt))) ||
-        !(rtol > 0) || !(atol > 0) || (form != HF_CHEM_PLAIN && form != HF_CHEM_PERSISTENT))
+    if (!ctx || !U || count < 0 || count > INT32_MAX || (!cell_index && comp_stride < count) ||
+        (!dt_cell && (!(dt > 0) || !std::isfinite(dt))) || !(rtol > 0) || !(atol > 0) ||
+        (form != HF_CHEM_PLAIN && form != HF_CHEM_PERSISTENT && form != 2))
         return fail(ctx, HF_ERR_ARG, "chem_advance: invalid batch extent, interval or tolerances");
     if (count == 0) return HF_OK;
     const cudaStream_t s = S(stream);
     const int nv = ctx->ns + 3;
-    const size_t need = sizeof(double) * (size_t)nv * count + sizeof(int) * (size_t)count;
-    char* w = static_cast<char*>(scratch(ctx, need));
+    // scratch: trial states | fail codes | queue order | bucket offsets
+    const size_t b_trial = sizeof(double) * (size_t)nv * count;
+    const size_t b_fail = (sizeof(int) * (size_t)count + 15) & ~size_t(15);
+    const size_t b_order = (sizeof(int32_t) * (size_t)count + 15) & ~size_t(15);
+    char* w = static_cast<char*>(scratch(ctx, b_trial + b_fail + b_order + 16 * sizeof(unsigned long long)));
     if (!w) return fail(ctx, HF_ERR_CUDA, "chem_advance: scratch allocation failed");
     double* trial = reinterpret_cast<double*>(w);
-    int* failv = reinterpret_cast<int*>(w + sizeof(double) * (size_t)nv * count);
+    int* failv = reinterpret_cast<int*>(w + b_trial);
+    int32_t* order = reinterpret_cast<int32_t*>(w + b_trial + b_fail);
+    unsigned long long* bins = reinterpret_cast<unsigned long long*>(w + b_trial + b_fail + b_order);
     HF_CUDA(reset_status(ctx, s));
     tic(ctx, 1, s);
-    HF_CUDA(launch_chem(ctx->ns, form, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, trial, failv, ctx->st,
-                        ctx->sm_count, s, &ctx->cnt.kernel_launches));
-    toc(ctx, s, 1);
+    const int64_t l0 = ctx->cnt.kernel_launches;
+    if (form == 2)
+        HF_CUDA(launch_chem_batched(ctx->ns, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol,
+                                    hist ? hist->h : nullptr, hist ? hist->cost : nullptr, order, bins, trial, failv,
+                                    ctx->st, ctx->sm_count, s, &ctx->cnt.kernel_launches));
+    else
+        HF_CUDA(launch_chem(ctx->ns, form, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, trial, failv,
+                            ctx->st, ctx->sm_count, s, &ctx->cnt.kernel_launches));
+    toc(ctx, s, ctx->cnt.kernel_launches - l0);
     HF_CUDA(read_status(ctx, s));
     ctx->cnt.chem_steps += (int64_t)ctx->st_host->steps;
     const unsigned f = ctx->st_host->flags;
@@ -415,6 +429,24 @@ hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int
     HF_CUDA(launch_chem_commit(ctx->ns, U, comp_stride, cell_index, count, trial, s, &ctx->cnt.kernel_launches));
     ctx->cnt.chem_cell_calls += count;
     return HF_OK;
+}
+
+hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index, int64_t count,
+                          double dt, const double* dt_cell, double rtol, double atol, int form, int64_t* first_failed,
+                          void* stream) {
+    if (form != HF_CHEM_PLAIN && form != HF_CHEM_PERSISTENT) {
+        if (first_failed) *first_failed = -1;
+        return fail(ctx, HF_ERR_ARG, "chem_advance: unknown form");
+    }
+    return chem_common(ctx, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, form, nullptr, first_failed,
+                       stream);
+}
+
+hf_status hf_chem_advance_batched(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index,
+                                  int64_t count, double dt, const double* dt_cell, double rtol, double atol,
+                                  const hf_chem_history* history, int64_t* first_failed, void* stream) {
+    return chem_common(ctx, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, 2, history, first_failed,
+                       stream);
 }
 
 hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U, double cfl,

@@ -13,6 +13,7 @@
 // they can be scaled for sensitivity checks; reaction structure, temperature
 // exponents and activation temperatures are compile-time constants of the
 // generated mechanism table, so every species index below is a register index.
+#include <cstdlib>
 #include <utility>
 #include "hf_device.cuh"
 #include "hf_internal.h"
@@ -302,6 +303,7 @@ struct ChemCell {
     static constexpr int N = NS - 1;
     double y[N], f0[N], J[N * N];
     double h, t, tend, rho, e, T, Tsave;
+    double mom[3];  // rho*u, rho*v, rho*E: chemistry leaves them unchanged
     int steps, attempts;
     bool rejectLast, rejectMore, needJ;
 };
@@ -322,7 +324,7 @@ __device__ __forceinline__ void comp(const double* y, double rho, double* z, dou
 
 // chemistry.cpp:36-53
 template <int NS>
-__device__ __forceinline__ bool chem_rhs(double rho, double e, double& T, const double* y, double* dy) {
+__device__ __noinline__ bool chem_rhs(double rho, double e, double& T, const double* y, double* dy) {
     double z[NS], C[NS], m[6];
     comp<NS>(y, rho, z, C);
     double Tn = T;
@@ -345,7 +347,7 @@ __device__ __forceinline__ bool chem_rhs(double rho, double e, double& T, const 
 }
 
 template <int NS>
-__device__ __forceinline__ bool chem_jac(double rho, double e, double& T, const double* y, double* J) {
+__device__ __noinline__ bool chem_jac(double rho, double e, double& T, const double* y, double* J) {
     constexpr int N = NS - 1, L = NS - 1;
     double z[NS], C[NS], m[6];
     comp<NS>(y, rho, z, C);
@@ -464,7 +466,7 @@ __device__ __forceinline__ void lu_solve(const double* A, const int* piv, double
 // Loads a cell and prepares the integration (chemistry.cpp:55-62 + the starting
 // step of the integrator).  Returns CELL_CONTINUE or CELL_FAIL.
 template <int NS>
-__device__ int cell_begin(ChemCell<NS>& c, const double* u, double dt, double rtol, double atol) {
+__device__ __noinline__ int cell_begin(ChemCell<NS>& c, const double* u, double dt, double rtol, double atol) {
     constexpr int N = NS - 1;
     if (!(dt > 0.0) || !isfinite(dt)) return CELL_FAIL;
     Props pr;
@@ -476,6 +478,9 @@ __device__ int cell_begin(ChemCell<NS>& c, const double* u, double dt, double rt
     const double uu = u[NS] * ir, vv = u[NS + 1] * ir;
     c.rho = rho;
     c.e = u[NS + 2] * ir - 0.5 * (uu * uu + vv * vv);
+    c.mom[0] = u[NS];
+    c.mom[1] = u[NS + 1];
+    c.mom[2] = u[NS + 2];
     c.T = pr.T;
 #pragma unroll
     for (int k = 0; k < N; ++k) c.y[k] = u[k] * ir;
@@ -513,7 +518,7 @@ __device__ int cell_begin(ChemCell<NS>& c, const double* u, double dt, double rt
 
 // One step attempt (the body of the KPP accept loop).
 template <int NS>
-__device__ int cell_attempt(ChemCell<NS>& c, double rtol, double atol) {
+__device__ __noinline__ int cell_attempt(ChemCell<NS>& c, double rtol, double atol) {
     constexpr int N = NS - 1;
     if (c.needJ) {
         if (c.steps >= MAX_STEPS) return CELL_MAXSTEPS;
@@ -607,8 +612,9 @@ __device__ int cell_attempt(ChemCell<NS>& c, double rtol, double atol) {
 }
 
 // chemistry.cpp:63-70: clip, close the mass with the last species, final check.
+// Writes the whole state u (momentum and energy as they came in).
 template <int NS>
-__device__ bool cell_end(const ChemCell<NS>& c, double* u) {
+__device__ __noinline__ bool cell_end(const ChemCell<NS>& c, double* u) {
     constexpr int N = NS - 1;
     double s = 0.0;
 #pragma unroll
@@ -619,8 +625,112 @@ __device__ bool cell_end(const ChemCell<NS>& c, double* u) {
         s += u[k];
     }
     u[N] = c.rho - s;
+    u[NS] = c.mom[0];
+    u[NS + 1] = c.mom[1];
+    u[NS + 2] = c.mom[2];
     Props pr;
     return properties<NS>(u, pr, c.T);
+}
+
+// ---------------------------------------------------------------- batched form
+// Batched-form start of a cell (extension to the reference's per-call CVODE
+// restart).  After f0 = f(y0) and J = df/dy at y0:
+//  * frozen-cell screen: in the scaled variables z_i = y_i / sc_i
+//    (sc_i = atol + rtol |y_i|), with a = ||J_z||_inf dt, if a <= 20,
+//    ||f0_z||_inf dt e^a <= 1 and ||f0_z||_inf dt a^2 e^a / 6 <= 1e-5, the interval
+//    is taken as one second-order Taylor step y1 = y0 + dt f0 + dt^2/2 J f0: for the
+//    linearised system its remainder sum_{k>=3} dt^k/k! J^(k-1) f0 is bounded by
+//    the last expression, i.e. below 1e-5 tolerance units;
+//  * otherwise the first step size is the cell's proposed step from the previous
+//    call (h_prev > 0), else the same starting-step estimate as cell_begin; the
+//    Jacobian just formed is the first step's Jacobian.
+// Returns CELL_DONE (screened), CELL_CONTINUE or CELL_FAIL.
+template <int NS>
+__device__ __noinline__ int cell_begin_batched(ChemCell<NS>& c, const double* u, double dt, double rtol, double atol,
+                                               double h_prev) {
+    constexpr int N = NS - 1;
+    if (!(dt > 0.0) || !isfinite(dt)) return CELL_FAIL;
+    Props pr;
+    if (!properties<NS>(u, pr, 1000.0)) return CELL_FAIL;
+    double rho = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) rho += u[k];
+    const double ir = 1.0 / rho;
+    const double uu = u[NS] * ir, vv = u[NS + 1] * ir;
+    c.rho = rho;
+    c.e = u[NS + 2] * ir - 0.5 * (uu * uu + vv * vv);
+    c.mom[0] = u[NS];
+    c.mom[1] = u[NS + 1];
+    c.mom[2] = u[NS + 2];
+    c.T = pr.T;
+#pragma unroll
+    for (int k = 0; k < N; ++k) c.y[k] = u[k] * ir;
+    if (!chem_rhs<NS>(c.rho, c.e, c.T, c.y, c.f0)) return CELL_FAIL;
+    if (!chem_jac<NS>(c.rho, c.e, c.T, c.y, c.J)) return CELL_FAIL;
+    c.Tsave = c.T;
+    c.t = 0.0;
+    c.tend = dt;
+    c.steps = 0;
+    c.attempts = 0;
+    c.rejectLast = c.rejectMore = false;
+    c.needJ = false;
+    double sc[N], fz = 0.0, jz = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        sc[i] = atol + rtol * fabs(c.y[i]);
+        fz = fmax(fz, fabs(c.f0[i]) / sc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        double r = 0.0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) r = fma(fabs(c.J[i * N + j]), sc[j], r);
+        jz = fmax(jz, r / sc[i]);
+    }
+    // remainder of the second-order Taylor step for the linearised system:
+    // ||R||_z <= fz dt * a^2 e^a / 6 with a = jz dt; the whole change stays below
+    // fz dt e^a <= 1 tolerance unit, so J is constant over the interval to far
+    // better than the tolerance
+    const double a = jz * dt;
+    const double ea = a <= 20.0 ? exp(a) : 1e300;
+    if (a <= 20.0 && fz * dt * ea <= 1.0 && fz * dt * a * a * ea <= 6e-5) {
+        double jf[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < N; ++j) v = fma(c.J[i * N + j], c.f0[j], v);
+            jf[i] = v;
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) c.y[i] = fma(0.5 * dt * dt, jf[i], fma(dt, c.f0[i], c.y[i]));
+        c.t = dt;
+        c.h = dt;
+        return CELL_DONE;
+    }
+    if (h_prev > 0.0 && isfinite(h_prev)) {
+        c.h = fmin(h_prev, dt);
+    } else {
+        const double Ts = c.T;
+        const double d0 = wrms<N>(c.y, c.y, c.y, rtol, atol), d1 = wrms<N>(c.f0, c.y, c.y, rtol, atol) * dt;
+        const double hh = d1 < 1e-5 ? 1.0 : fmin(1.0, 0.01 * d0 / d1);
+        double yn[N], fy[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) yn[i] = c.y[i] + hh * dt * c.f0[i];
+        double d2;
+        if (chem_rhs<NS>(c.rho, c.e, c.T, yn, fy)) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) fy[i] = (fy[i] - c.f0[i]) / hh;
+            d2 = wrms<N>(fy, c.y, c.y, rtol, atol);
+        } else {
+            d2 = 1e30;
+        }
+        c.T = Ts;
+        const double mx = fmax(d1, d2);
+        const double h1 = mx <= 1e-15 ? 1.0 : pow(0.01 / mx, 0.2);
+        c.h = fmin(fmin(100.0 * hh, h1), 1.0) * dt;
+    }
+    return CELL_CONTINUE;
 }
 
 // ---------------------------------------------------------------- kernels
@@ -731,6 +841,162 @@ __global__ void k_chem_commit(double* __restrict__ U, int64_t cs, const int64_t*
     const int64_t b = cell_index ? cell_index[i] : i;
 #pragma unroll
     for (int n = 0; n < NS + 3; ++n) U[b + n * cs] = trial[n * count + i];
+}
+
+// Batched form: the persistent lane-refill loop of k_chem_persistent over a work
+// queue ordered most-expensive-first (order[]), starting each cell with
+// cell_begin_batched, and recording per cell the attempts taken (cost[]) and the
+// controller's proposed next step (h_hist[]) for the next call.
+template <int NS, int MINB>
+__global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restrict__ U, int64_t cs,
+                                                     const int64_t* __restrict__ cell_index,
+                                                     const int32_t* __restrict__ order, int64_t count, double dt,
+                                                     const double* __restrict__ dt_cell, double rtol, double atol,
+                                                     double* __restrict__ trial, int* __restrict__ fail,
+                                                     double* __restrict__ h_hist, int32_t* __restrict__ cost,
+                                                     DevStatus* st) {
+    const unsigned lane = threadIdx.x & 31;
+    ChemCell<NS> c;
+    int64_t cell = -1;
+    bool active = false, drained = false;
+    unsigned long long my_attempts = 0;
+    for (;;) {
+        if (!drained) {
+            const unsigned need = __ballot_sync(0xffffffffu, !active);
+            bool none = false;
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                unsigned long long base = 0;
+                if ((int)lane == leader) base = atomicAdd(&st->counter, (unsigned long long)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!active) {
+                    const int64_t q = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
+                    if (q < count) {
+                        const int64_t k = order ? (int64_t)order[q] : q;
+                        cell = k;
+                        double u[NS + 3];
+                        load_cell<NS>(U, cs, cell_index ? cell_index[k] : k, u);
+                        const int r = cell_begin_batched<NS>(c, u, dt_cell ? dt_cell[k] : dt, rtol, atol,
+                                                             h_hist ? h_hist[k] : 0.0);
+                        if (r == CELL_CONTINUE) {
+                            active = true;
+                        } else if (r == CELL_DONE && cell_end<NS>(c, u)) {
+#pragma unroll
+                            for (int n = 0; n < NS + 3; ++n) trial[n * count + k] = u[n];
+                            fail[k] = 0;
+                            if (cost) cost[k] = 0;
+                        } else {
+                            report(st, fail, k, CELL_FAIL);
+                        }
+                    } else {
+                        none = true;
+                    }
+                }
+            }
+            drained = __any_sync(0xffffffffu, none);
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (drained) break;
+            continue;
+        }
+        if (active) {
+            const int r = cell_attempt<NS>(c, rtol, atol);
+            if (r != CELL_CONTINUE) {
+                my_attempts += c.attempts;
+                double u[NS + 3];
+                if (r == CELL_DONE && cell_end<NS>(c, u)) {
+#pragma unroll
+                    for (int n = 0; n < NS + 3; ++n) trial[n * count + cell] = u[n];
+                    fail[cell] = 0;
+                    if (h_hist) h_hist[cell] = c.h;
+                    if (cost) cost[cell] = c.attempts;
+                } else {
+                    report(st, fail, cell, r == CELL_MAXSTEPS ? CELL_MAXSTEPS : CELL_FAIL);
+                }
+                active = false;
+            }
+        }
+    }
+    if (my_attempts) atomicAdd(&st->steps, my_attempts);
+}
+
+// Work-queue order: counting sort of cells by bucket = floor(log2(cost + 1)) (16
+// buckets), most expensive bucket first.  Cells of one bucket keep no particular
+// order; each cell's result does not depend on its position.
+constexpr int NBUCKET = 16;
+__device__ __forceinline__ int cost_bucket(int32_t c) {
+    const int b = 31 - __clz((unsigned)c + 1u);
+    return min(b, NBUCKET - 1);
+}
+__global__ void k_order_hist(const int32_t* __restrict__ cost, int64_t count, unsigned long long* __restrict__ bins) {
+    __shared__ unsigned int sb[NBUCKET];
+    if (threadIdx.x < NBUCKET) sb[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&sb[cost_bucket(max(cost[i], 0))], 1u);
+    __syncthreads();
+    if (threadIdx.x < NBUCKET && sb[threadIdx.x]) atomicAdd(&bins[threadIdx.x], (unsigned long long)sb[threadIdx.x]);
+}
+__global__ void k_order_scan(unsigned long long* bins) {
+    // bins[b] -> start offset of bucket b, descending buckets first
+    unsigned long long off = 0;
+    for (int b = NBUCKET - 1; b >= 0; --b) {
+        const unsigned long long n = bins[b];
+        bins[b] = off;
+        off += n;
+    }
+}
+__global__ void k_order_scatter(const int32_t* __restrict__ cost, int64_t count, unsigned long long* __restrict__ bins,
+                                int32_t* __restrict__ order) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long pos = atomicAdd(&bins[cost_bucket(max(cost[i], 0))], 1ull);
+        order[pos] = (int32_t)i;
+    }
+}
+
+template <int NS>
+static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
+                                     const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
+                                     int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
+                                     int sm_count, cudaStream_t s, int64_t* launches) {
+    if (cost && order) {
+        cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * NBUCKET, s);
+        if (e != cudaSuccess) return e;
+        const int g = sm_count * 4;
+        k_order_hist<<<g, 256, 0, s>>>(cost, count, bins);
+        k_order_scan<<<1, 1, 0, s>>>(bins);
+        k_order_scatter<<<g, 256, 0, s>>>(cost, count, bins, order);
+        *launches += 3;
+    } else {
+        order = nullptr;
+    }
+    // register budget of the queue kernel: 255 (4 blocks of 64 per SM) or 128 (8 blocks);
+    // HF_CHEM_MINB=8 selects the second.  Both run the same per-cell code.
+    static const int minb = [] {
+        const char* e = getenv("HF_CHEM_MINB");
+        return (e && atoi(e) == 8) ? 8 : 4;
+    }();
+    auto kern = minb == 8 ? k_chem_batched<NS, 8> : k_chem_batched<NS, 4>;
+    const int bs = 64;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = (int64_t)sm_count * per_sm;
+    const int64_t need = (count + bs - 1) / bs;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    kern<<<(unsigned)blocks, bs, 0, s>>>(U, cs, idx, order, count, dt, dtc, rtol, atol, trial, fail, h_hist, cost, st);
+    ++*launches;
+    return cudaGetLastError();
+}
+cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
+                                const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
+                                int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
+                                int sm_count, cudaStream_t s, int64_t* launches) {
+    return ns == 9 ? chem_batched_impl<9>(U, cs, idx, count, dt, dtc, rtol, atol, h_hist, cost, order, bins, trial,
+                                          fail, st, sm_count, s, launches)
+                   : chem_batched_impl<10>(U, cs, idx, count, dt, dtc, rtol, atol, h_hist, cost, order, bins, trial,
+                                           fail, st, sm_count, s, launches);
 }
 
 template <int NS>

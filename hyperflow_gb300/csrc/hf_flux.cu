@@ -488,7 +488,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
         void* p = nullptr;
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
             fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
     }

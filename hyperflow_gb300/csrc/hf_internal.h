@@ -85,6 +85,10 @@ cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const 
                         int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                         double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
                         int64_t* launches);
+cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
+                                const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
+                                int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
+                                int sm_count, cudaStream_t s, int64_t* launches);
 cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
                                int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
 

@@ -18,6 +18,7 @@ struct hf_stepper {
     int flux_form = HF_FLUX_FUSED, chem_form = HF_CHEM_PERSISTENT;
     double* buf[4] = {nullptr, nullptr, nullptr, nullptr};  // [0] = current state
     int64_t* cells = nullptr;                                // valid-cell gather list
+    hf_chem_history hist{nullptr, nullptr};                  // batched chemistry history
     double time = 0.0;
 };
 
@@ -88,6 +89,13 @@ hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0
         hf_stepper_destroy(st);
         return HF_ERR_CUDA;
     }
+    if (cudaMalloc(&st->hist.h, sizeof(double) * nc) != cudaSuccess ||
+        cudaMalloc(&st->hist.cost, sizeof(int32_t) * nc) != cudaSuccess ||
+        cudaMemset(st->hist.h, 0, sizeof(double) * nc) != cudaSuccess ||
+        cudaMemset(st->hist.cost, 0, sizeof(int32_t) * nc) != cudaSuccess) {
+        hf_stepper_destroy(st);
+        return HF_ERR_CUDA;
+    }
     if (U0) {
         for (int n = 0; n < st->nv; ++n) {
             cudaError_t e = cudaMemcpy2D(st->buf[0] + n * P.comp_stride + P.ng * P.pitch + P.ng, P.pitch * sizeof(double),
@@ -105,6 +113,8 @@ void hf_stepper_destroy(hf_stepper* st) {
     for (auto b : st->buf)
         if (b) cudaFree(b);
     if (st->cells) cudaFree(st->cells);
+    if (st->hist.h) cudaFree(st->hist.h);
+    if (st->hist.cost) cudaFree(st->hist.cost);
     delete st;
 }
 
@@ -124,8 +134,13 @@ hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) 
         hf_status r = flow(st, S0, T1, X, 0.5 * h, s);
         if (r == HF_OK && st->chemistry) {
             int64_t first = -1;
-            r = hf_chem_advance(st->ctx, X, st->P.comp_stride, st->cells, (int64_t)st->P.nx * st->P.ny, h, nullptr,
-                                st->rtol, st->atol, st->chem_form, &first, s);
+            const int64_t nc = (int64_t)st->P.nx * st->P.ny;
+            if (st->chem_form == HF_CHEM_PERSISTENT)
+                r = hf_chem_advance_batched(st->ctx, X, st->P.comp_stride, st->cells, nc, h, nullptr, st->rtol,
+                                            st->atol, &st->hist, &first, s);
+            else
+                r = hf_chem_advance(st->ctx, X, st->P.comp_stride, st->cells, nc, h, nullptr, st->rtol, st->atol,
+                                    st->chem_form, &first, s);
             if (r == HF_OK) {
                 int64_t bad = -1;
                 r = hf_validate(st->ctx, &st->L, &st->P, 1, X, &bad, s);

@@ -237,12 +237,20 @@ class ConservativeInterp:
 class ChemistryBatch:
     """ChemistryBatch (src/chemistry_batch.hpp): all-or-nothing advance of a batch of cells.
 
-    form: "plain" (one thread per cell) or "persistent" (device work queue)."""
+    form: "plain" (one thread per cell), "persistent" (device work queue; the same
+    per-cell step sequence as plain), or "batched" (persistent queue plus frozen-cell
+    screening, warm-started step sizes and a cost-ordered queue, using per-cell
+    history kept by this object between calls)."""
 
-    def __init__(self, ctx, form="persistent", rtol=1e-8, atol=1e-15):
+    FORMS = {"plain": L.HF_CHEM_PLAIN, "persistent": L.HF_CHEM_PERSISTENT, "batched": -1}
+
+    def __init__(self, ctx, form="batched", rtol=1e-8, atol=1e-15):
         self.ctx = ctx
-        self.form = {"plain": L.HF_CHEM_PLAIN, "persistent": L.HF_CHEM_PERSISTENT}[form]
+        if form not in self.FORMS:
+            raise ValueError("unknown chemistry form %r" % form)
+        self.form = form
         self.rtol, self.atol = rtol, atol
+        self.history = None
 
     def advance(self, field, dt, count=None, dt_cell=None, cell_index=None, comp_stride=None):
         """field: (NV, n) float64 CUDA tensor (SoA), advanced in place over dt.
@@ -259,13 +267,21 @@ class ChemistryBatch:
         else:
             n = cell_index.numel() if count is None else int(count)
             cs = int(comp_stride)
-        dtc = None
         if dt_cell is not None:
             _need_cuda64(dt_cell, "dt_cell")
         first = ctypes.c_int64(-1)
-        st = self.ctx.lib.hf_chem_advance(self.ctx.h, _ptr(field), cs, _ptr(cell_index), n, float(dt),
-                                          _ptr(dt_cell), float(self.rtol), float(self.atol), self.form,
-                                          ctypes.byref(first), _stream())
+        if self.form == "batched":
+            if self.history is None or self.history[0].numel() != n:
+                self.history = (torch.zeros(n, dtype=torch.float64, device=field.device),
+                                torch.zeros(n, dtype=torch.int32, device=field.device))
+            hist = L.ChemHistory(self.history[0].data_ptr(), self.history[1].data_ptr())
+            st = self.ctx.lib.hf_chem_advance_batched(self.ctx.h, _ptr(field), cs, _ptr(cell_index), n, float(dt),
+                                                      _ptr(dt_cell), float(self.rtol), float(self.atol),
+                                                      ctypes.byref(hist), ctypes.byref(first), _stream())
+        else:
+            st = self.ctx.lib.hf_chem_advance(self.ctx.h, _ptr(field), cs, _ptr(cell_index), n, float(dt),
+                                              _ptr(dt_cell), float(self.rtol), float(self.atol),
+                                              self.FORMS[self.form], ctypes.byref(first), _stream())
         if st in (L.HF_ERR_CHEM_FAIL, L.HF_ERR_MAXSTEPS):
             e = RuntimeError("chemistry cell %d: %s" % (first.value,
                                                         (self.ctx.lib.hf_last_error(self.ctx.h) or b"").decode()))
@@ -280,10 +296,13 @@ class ChemistryBatch:
 class Stepper:
     """Strang-split reacting-Euler stepper on a uniform one-patch level.
 
+    flux: "fused" or "plain"; chem: "batched" (work queue with per-cell history) or
+    "plain" (one thread per cell).
+
     step(): flow(dt/2); react(dt); flow(dt/2) with rollback and dt halving
     (BlockAMR.cpp:409-419).  U0: (NV, ny, nx) float64 CUDA tensor."""
 
-    def __init__(self, ctx, level, U0, chemistry=True, rtol=1e-8, atol=1e-15, flux="fused", chem="persistent"):
+    def __init__(self, ctx, level, U0, chemistry=True, rtol=1e-8, atol=1e-15, flux="fused", chem="batched"):
         _need_cuda64(U0, "U0")
         self.ctx = ctx
         self.level = level
@@ -291,7 +310,7 @@ class Stepper:
         U0 = U0.contiguous()
         h = ctypes.c_void_p()
         ff = {"plain": L.HF_FLUX_PLAIN, "fused": L.HF_FLUX_FUSED}[flux]
-        cf = {"plain": L.HF_CHEM_PLAIN, "persistent": L.HF_CHEM_PERSISTENT}[chem]
+        cf = {"plain": L.HF_CHEM_PLAIN, "batched": L.HF_CHEM_PERSISTENT, "persistent": L.HF_CHEM_PERSISTENT}[chem]
         torch.cuda.synchronize()
         ctx.check(ctx.lib.hf_stepper_create(ctx.h, ctypes.byref(level), _ptr(U0), int(bool(chemistry)), float(rtol),
                                             float(atol), ff, cf, ctypes.byref(h)), "stepper_create")

@@ -171,6 +171,26 @@ HF_EXPORT hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride,
                           int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                           int form, int64_t* first_failed, void* stream);
 
+/* Per-cell integrator history of the batched chemistry form (extension: the reference's
+ * CVODE restarts every cell from scratch on each call).  Caller-owned device arrays of
+ * count entries, zero-initialised before the first call.  h: the step size the controller
+ * proposed after the cell's last interval (warm start of the next call); cost: the cell's
+ * step attempts in the last call (orders the work queue most-expensive-first). */
+typedef struct hf_chem_history {
+    double* h;
+    int32_t* cost;
+} hf_chem_history;
+
+/* Batched chemistry: the persistent work-queue kernel plus a frozen-cell screen (a cell whose
+ * scaled derivative and Jacobian norms over dt are tiny takes one second-order Taylor step,
+ * truncation error below 2e-5 tolerance units), warm-started step sizes and a cost-ordered
+ * queue.  Same arguments, semantics and errors as hf_chem_advance (ChemistryBatch::advance,
+ * chemistry_batch.cpp:21-50); history may be NULL. */
+HF_EXPORT hf_status hf_chem_advance_batched(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index,
+                                            int64_t count, double dt, const double* dt_cell, double rtol,
+                                            double atol, const hf_chem_history* history, int64_t* first_failed,
+                                            void* stream);
+
 /* ---- reductions ---- */
 /* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the valid cells of the patches:
  * *dt = cfl / max((|u|+a)/dx + (|v|+a)/dy).  HF_ERR_INADMISSIBLE if a cell is not. */

@@ -44,9 +44,16 @@ def test_hllc_matches_oracle(gpu, oracle, direction):
     n = 300
     L = H.random_states(n, seed=2)
     R = H.random_states(n, seed=3)
-    # include supersonic and near-identical pairs
+    # include near-identical pairs and supersonic pairs (both sides fast, same direction)
     R[:20] = L[:20] * (1 + 1e-3)
-    L[20:40, 9 + direction] *= 4.0
+    L[20:40] = H.random_states(20, seed=4, T=(300.0, 600.0), speed=1.0)
+    R[20:40] = L[20:40]
+    for k in range(20, 40):
+        sgn = 1.0 if k % 2 else -1.0
+        for q in (L, R):
+            rho = q[k, :9].sum()
+            q[k, 11] += 0.5 * rho * 3000.0 ** 2
+            q[k, 9 + direction] = sgn * rho * 3000.0
     pl = np.stack(oracle.properties(L)[:3])
     pr = np.stack(oracle.properties(R)[:3])
     f = hf.hllc(gpu, cuda(L.T), cuda(R.T), cuda(pl), cuda(pr), direction).cpu().numpy().T
@@ -234,7 +241,7 @@ def _compare_chem(got, ref):
     return t_err, y_err
 
 
-@pytest.mark.parametrize("form", ["plain", "persistent"])
+@pytest.mark.parametrize("form", ["plain", "persistent", "batched"])
 def test_chemistry_matches_oracle(gpu, oracle, form):
     import hyperflow_gb300 as hf
     U, dt = _chem_cells(96, seed=3)
@@ -255,6 +262,28 @@ def test_chemistry_forms_identical(gpu):
     hf.ChemistryBatch(gpu, "plain").advance(a, 0.0, dt_cell=cuda(dt))
     hf.ChemistryBatch(gpu, "persistent").advance(b, 0.0, dt_cell=cuda(dt))
     assert torch.equal(a, b)
+
+
+def test_batched_history_and_screen(gpu, oracle):
+    """Batched form over two consecutive intervals (warm-started step sizes, cost-ordered
+    queue) on a mix of frozen cold cells and igniting hot cells, against the oracle."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import mechanism as M
+    X = np.array([2.0, 1.0, 0, 0, 0, 0, 0, 0, 3.76]) / 6.76
+    cells = [M.primitive(298.0, 101325.0, X=X, ns=9), M.primitive(3000.0, 40 * 101325.0, X=X, ns=9),
+             M.primitive(1100.0, 2e5, X=X, ns=9), M.primitive(2400.0, 1e5, X=X, ns=9)]
+    U = np.array([cells[k % 4] for k in range(64)])
+    ref = U.copy()
+    field = cuda(U.T.copy())
+    cb = hf.ChemistryBatch(gpu, "batched")
+    for _ in range(2):
+        ref, bad, _ = oracle.chem_batch(ref, 1e-8)
+        assert bad == -1
+        cb.advance(field, 1e-8)
+    t_err, y_err = _compare_chem(field.cpu().numpy().T, ref)
+    assert t_err < 1e-6 and y_err < 1e-8, (t_err, y_err)
+    cost = cb.history[1].cpu().numpy()
+    assert cost[0] == 0 and cost[1] > 10   # cold cell screened, hot cell integrated
 
 
 def test_chemistry_zero_dimensional_against_tight(gpu, oracle):
