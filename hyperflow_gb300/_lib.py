@@ -64,6 +64,7 @@ SIGNATURES = [
                               _vp, _d, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
+    ("hf_chem_advance_noalloc", _i32, [ctypes.c_int, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.POINTER(_i64), _vp]),
     ("hf_cfl_dt", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d, _dp, _vp]),
     ("hf_validate", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp,
                            ctypes.POINTER(_i64), _vp]),

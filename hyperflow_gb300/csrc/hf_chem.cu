@@ -1035,4 +1035,79 @@ cudaError_t launch_chem_commit(int ns, double* U, int64_t cs, const int64_t* idx
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- allocation-free entry
+// Scratch of hf_chem_advance_noalloc: a file-scope device array of fixed size, so the
+// entry point allocates nothing.  Host code reaches it only through the device address
+// that cudaGetSymbolAddress returns (the symbol itself is a host-side stand-in).
+struct NoAllocScratch {
+    DevStatus st;
+    int fail[HF_NOALLOC_MAX_CELLS];
+    double trial[(NS_MAX + 3) * HF_NOALLOC_MAX_CELLS];
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
 }  // namespace hf
+
+#include <mutex>
+
+namespace {
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+hf::NoAllocScratch* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Once per device, with that device current: the array's device address, and the
+// rate constants if no context has loaded them on this device yet.
+cudaError_t noalloc_setup(int dev, hf::NoAllocScratch** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        hf::NoAllocScratch* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, hf::g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        double a0 = 0.0;
+        e = cudaMemcpyFromSymbol(&a0, hf::c_A, sizeof(double));
+        if (e != cudaSuccess) return e;
+        if (a0 == 0.0) {
+            e = hf::chem_set_rate_scale(nullptr);
+            if (e != cudaSuccess) return e;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+extern "C" hf_status hf_chem_advance_noalloc(int nspecies, double* U, int64_t comp_stride, const int64_t* cell_index,
+                                             int64_t count, double dt, const double* dt_cell, double rtol, double atol,
+                                             int64_t* first_failed, void* stream) {
+    using namespace hf;
+    if (first_failed) *first_failed = -1;
+    if ((nspecies != 9 && nspecies != 10) || !U || count < 0 || count > HF_NOALLOC_MAX_CELLS ||
+        (!cell_index && comp_stride < count) || (!dt_cell && (!(dt > 0) || !isfinite(dt))) || !(rtol > 0) ||
+        !(atol > 0))
+        return HF_ERR_ARG;
+    if (count == 0) return HF_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return HF_ERR_CUDA;
+    NoAllocScratch* S = nullptr;
+    if (noalloc_setup(dev, &S) != cudaSuccess) return HF_ERR_CUDA;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(&S->st, 0, sizeof(DevStatus), s) != cudaSuccess ||
+        cudaMemsetAsync(&S->st.bad_cell, 0xff, sizeof(unsigned long long), s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    int64_t launches = 0;
+    if (launch_chem(nspecies, HF_CHEM_PLAIN, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol, S->trial,
+                    S->fail, &S->st, 1, s, &launches) != cudaSuccess)
+        return HF_ERR_CUDA;
+    DevStatus h;
+    if (cudaMemcpyAsync(&h, &S->st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    if (h.flags & (ST_CHEM_FAIL | ST_MAXSTEPS)) {
+        if (first_failed) *first_failed = (int64_t)h.bad_cell;
+        return (h.flags & ST_CHEM_FAIL) ? HF_ERR_CHEM_FAIL : HF_ERR_MAXSTEPS;
+    }
+    if (launch_chem_commit(nspecies, U, comp_stride, cell_index, count, S->trial, s, &launches) != cudaSuccess)
+        return HF_ERR_CUDA;
+    return HF_OK;
+}

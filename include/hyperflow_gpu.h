@@ -191,6 +191,28 @@ HF_EXPORT hf_status hf_chem_advance_batched(hf_ctx* ctx, double* U, int64_t comp
                                             double atol, const hf_chem_history* history, int64_t* first_failed,
                                             void* stream);
 
+/* Chemistry without any device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: code running while a stream is being captured
+ * into a CUDA graph, host code that must not synchronise the device through the allocator,
+ * or an embedding application whose memory budget is fixed up front and reserved for its
+ * own pool.  It needs no hf_ctx (hf_init allocates).  It runs the plain form of
+ * hf_chem_advance (one thread per cell, same results, same all-or-nothing semantics and
+ * error codes) with its scratch (trial states, failure codes, status word) in one
+ * statically sized device array that every GPU loading this library holds until the
+ * process exits: HF_NOALLOC_MAX_CELLS cells, about 1.8 MB.
+ *   - nspecies: 9 (H2_Li) or 10 (H2_Li+AR); count > HF_NOALLOC_MAX_CELLS -> HF_ERR_ARG.
+ *   - The first call on a device (the current device) looks up the array's device address
+ *     and, if no hf_ctx has done so on that device, loads the rate constants; make that
+ *     first call before any stream capture.
+ *   - Every call uses the same array: calls that overlap on the GPU (other streams or
+ *     threads) race.  Each call clears the status word it needs before launching.
+ * Arguments as hf_chem_advance without ctx and form. */
+#define HF_NOALLOC_MAX_CELLS 16384
+HF_EXPORT hf_status hf_chem_advance_noalloc(int nspecies, double* U, int64_t comp_stride, const int64_t* cell_index,
+                                            int64_t count, double dt, const double* dt_cell, double rtol,
+                                            double atol, int64_t* first_failed, void* stream);
+
 /* ---- reductions ---- */
 /* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the valid cells of the patches:
  * *dt = cfl / max((|u|+a)/dx + (|v|+a)/dy).  HF_ERR_INADMISSIBLE if a cell is not. */
