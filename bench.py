@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--flux", default="fused", choices=["fused", "plain"], help="flux form of the headline run")
     p.add_argument("--chem", default="persistent", choices=["persistent", "plain"],
                    help="chemistry form of the headline run")
+    p.add_argument("--chem-cells", type=int, default=1 << 18,
+                   help="cells of the extra chemistry-only batch (0 = skip)")
     p.add_argument("--nx", type=int, default=NX)
     p.add_argument("--ny", type=int, default=NY)
     return p.parse_args()
@@ -221,6 +223,28 @@ def run_ours(args):
         plain = {"value": world * cells * ps / (pms * 1e-3), "ms_per_step": pms / ps, "steps": ps,
                  "chem_ms_per_step": ptm["chem"][0] / ps, "flux_ms_per_step": ptm["flux"][0] / ps}
 
+    chem_batch = None
+    if args.chem_cells > 0:
+        # chemistry-only batch of independent 0D cells with very uneven stiffness
+        # (T ~ U[800,2500] K, p ~ logU[0.1,10] atm, phi ~ logU[0.3,3], Ar ~ U[0,0.8],
+        # dt ~ logU[1e-7,1e-6] s): one all-or-nothing advance per form, same inputs
+        Uc, dtc_np = W.chem_batch(args.chem_cells, seed=11, diluent="AR")
+        dtc = torch.from_numpy(dtc_np).cuda()
+        chem_batch = {"cells": args.chem_cells}
+        for form in ("batched", "plain"):
+            field = torch.from_numpy(Uc).cuda()
+            cb = hf.ChemistryBatch(ctx, form)
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            cb.advance(field, 0.0, dt_cell=dtc)
+            e1.record()
+            barrier()
+            cms = max_over_ranks(e0.elapsed_time(e1))
+            chem_batch[form] = {"ms": cms, "cells_per_s": world * args.chem_cells / (cms * 1e-3)}
+            del field
+        chem_batch["batched_over_plain"] = chem_batch["plain"]["ms"] / chem_batch["batched"]["ms"]
+
     e2e = None
     if not args.no_e2e:
         st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=args.flux, chem=args.chem)
@@ -275,6 +299,7 @@ def run_ours(args):
                                   "other": tm["other"][0] / args.steps},
         "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
         "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
+        "chem_batch_uneven": chem_batch,
         "roofline": roof, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -974,9 +974,13 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
     // HF_CHEM_MINB=8 selects the second.  Both run the same per-cell code.
     static const int minb = [] {
         const char* e = getenv("HF_CHEM_MINB");
-        return (e && atoi(e) == 8) ? 8 : 4;
+        const int v = e ? atoi(e) : 4;
+        return (v == 5 || v == 6 || v == 8) ? v : 4;
     }();
-    auto kern = minb == 8 ? k_chem_batched<NS, 8> : k_chem_batched<NS, 4>;
+    auto kern = minb == 8   ? k_chem_batched<NS, 8>
+                : minb == 6 ? k_chem_batched<NS, 6>
+                : minb == 5 ? k_chem_batched<NS, 5>
+                            : k_chem_batched<NS, 4>;
     const int bs = 64;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
