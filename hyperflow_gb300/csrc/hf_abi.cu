@@ -82,6 +82,7 @@ cudaError_t read_status(hf_ctx* ctx, cudaStream_t s) {
     if (e == cudaSuccess && ctx->pending) {
         float t = 0.f;
         if (cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->ms[ctx->pending_class] += t;
+        else (void)cudaGetLastError();  // leave no pending error for the caller's next call
         ctx->pending = false;
     }
     return e;
@@ -138,6 +139,21 @@ namespace hf {
 void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries) {
     ctx->cnt.first_order_stages += first_order_stages;
     ctx->cnt.retries += retries;
+}
+void ctx_add_launches(hf_ctx* ctx, int64_t kernels, int64_t chem_cells, int64_t chem_steps) {
+    ctx->cnt.kernel_launches += kernels;
+    ctx->cnt.chem_cell_calls += chem_cells;
+    ctx->cnt.chem_steps += chem_steps;
+}
+bool ctx_timing_enabled(const hf_ctx* ctx) { return ctx->timing; }
+void ctx_add_timing(hf_ctx* ctx, double flux_ms, double chem_ms, double other_ms, int64_t flux_launches,
+                    int64_t chem_launches, int64_t other_launches) {
+    ctx->ms[0] += flux_ms;
+    ctx->ms[1] += chem_ms;
+    ctx->ms[2] += other_ms;
+    ctx->launches[0] += flux_launches;
+    ctx->launches[1] += chem_launches;
+    ctx->launches[2] += other_launches;
 }
 }  // namespace hf
 
@@ -333,7 +349,7 @@ hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* pat
         if (form == HF_FLUX_FUSED) {
             const void* tm = tensor_map(ctx, U_in, patches[0]);
             if (!tm) return fail(ctx, HF_ERR_ARG, "flux_update: TMA descriptor rejected (alignment/pitch)");
-            HF_CUDA(launch_flux_fused(ctx->ns, L, patches[0], tm, U_in, uold, U_out, h, first_order, 0, ctx->st, s,
+            HF_CUDA(launch_flux_fused(ctx->ns, L, patches[0], tm, U_in, uold, U_out, h, nullptr, first_order, 0, ctx->st, s,
                                       &ctx->cnt.kernel_launches));
         } else {
             int64_t base = 0, ox = 0, oy = 0;
@@ -409,7 +425,7 @@ static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const 
     tic(ctx, 1, s);
     const int64_t l0 = ctx->cnt.kernel_launches;
     if (form == 2)
-        HF_CUDA(launch_chem_batched(ctx->ns, U, comp_stride, cell_index, count, dt, dt_cell, rtol, atol,
+        HF_CUDA(launch_chem_batched(ctx->ns, U, comp_stride, cell_index, count, dt, nullptr, dt_cell, rtol, atol,
                                     hist ? hist->h : nullptr, hist ? hist->cost : nullptr, order, bins, trial, failv,
                                     ctx->st, ctx->sm_count, s, &ctx->cnt.kernel_launches));
     else

@@ -851,11 +851,13 @@ template <int NS, int MINB>
 __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restrict__ U, int64_t cs,
                                                      const int64_t* __restrict__ cell_index,
                                                      const int32_t* __restrict__ order, int64_t count, double dt,
+                                                     const double* __restrict__ dt_dev,
                                                      const double* __restrict__ dt_cell, double rtol, double atol,
                                                      double* __restrict__ trial, int* __restrict__ fail,
                                                      double* __restrict__ h_hist, int32_t* __restrict__ cost,
                                                      DevStatus* st) {
     const unsigned lane = threadIdx.x & 31;
+    if (dt_dev) dt = *dt_dev;  // interval from device memory (graph-captured steps)
     ChemCell<NS> c;
     int64_t cell = -1;
     bool active = false, drained = false;
@@ -956,9 +958,10 @@ __global__ void k_order_scatter(const int32_t* __restrict__ cost, int64_t count,
 
 template <int NS>
 static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
-                                     const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
-                                     int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
-                                     int sm_count, cudaStream_t s, int64_t* launches) {
+                                     const double* dt_dev, const double* dtc, double rtol, double atol,
+                                     double* h_hist, int32_t* cost, int32_t* order, unsigned long long* bins,
+                                     double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
+                                     int64_t* launches) {
     if (cost && order) {
         cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * NBUCKET, s);
         if (e != cudaSuccess) return e;
@@ -989,18 +992,19 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
     const int64_t need = (count + bs - 1) / bs;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    kern<<<(unsigned)blocks, bs, 0, s>>>(U, cs, idx, order, count, dt, dtc, rtol, atol, trial, fail, h_hist, cost, st);
+    kern<<<(unsigned)blocks, bs, 0, s>>>(U, cs, idx, order, count, dt, dt_dev, dtc, rtol, atol, trial, fail, h_hist,
+                                         cost, st);
     ++*launches;
     return cudaGetLastError();
 }
 cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
-                                const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
-                                int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
-                                int sm_count, cudaStream_t s, int64_t* launches) {
-    return ns == 9 ? chem_batched_impl<9>(U, cs, idx, count, dt, dtc, rtol, atol, h_hist, cost, order, bins, trial,
-                                          fail, st, sm_count, s, launches)
-                   : chem_batched_impl<10>(U, cs, idx, count, dt, dtc, rtol, atol, h_hist, cost, order, bins, trial,
-                                           fail, st, sm_count, s, launches);
+                                const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,
+                                int32_t* cost, int32_t* order, unsigned long long* bins, double* trial, int* fail,
+                                DevStatus* st, int sm_count, cudaStream_t s, int64_t* launches) {
+    return ns == 9 ? chem_batched_impl<9>(U, cs, idx, count, dt, dt_dev, dtc, rtol, atol, h_hist, cost, order, bins,
+                                          trial, fail, st, sm_count, s, launches)
+                   : chem_batched_impl<10>(U, cs, idx, count, dt, dt_dev, dtc, rtol, atol, h_hist, cost, order, bins,
+                                           trial, fail, st, sm_count, s, launches);
 }
 
 template <int NS>

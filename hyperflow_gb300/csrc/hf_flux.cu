@@ -327,9 +327,15 @@ struct FusedSmem {
 template <int NS>
 __global__ void __launch_bounds__(NTHR) k_flux_fused(const __grid_constant__ CUtensorMap tmap, Level L, hf_patch P,
                                                      const double* __restrict__ Uin, const double* __restrict__ Uold,
-                                                     double* __restrict__ Uout, double cx, double cy, int first_order,
+                                                     double* __restrict__ Uout, double cx, double cy,
+                                                     const double* __restrict__ hdev, int first_order,
                                                      int64_t cell_base, DevStatus* st) {
     constexpr int NV = NS + 3;
+    if (hdev) {  // stage length from device memory (graph-captured steps)
+        const double h = *hdev;
+        cx = h / L.dx;
+        cy = h / L.dy;
+    }
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ int s_fail;
@@ -512,8 +518,8 @@ bool make_tensor_map(void* tmap, const double* base, const hf_patch& P, int nv) 
 
 template <int NS>
 static cudaError_t flux_fused_impl(const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
-                                   const double* Uold, double* Uout, double h, int first_order, int64_t cell_base,
-                                   DevStatus* st, cudaStream_t s, int64_t* launches) {
+                                   const double* Uold, double* Uout, double h, const double* hdev, int first_order,
+                                   int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches) {
     static bool attr = false;
     const size_t smem = FusedSmem<NS>::bytes;
     if (!attr) {
@@ -523,15 +529,30 @@ static cudaError_t flux_fused_impl(const Level& L, const hf_patch& P, const void
     }
     dim3 grid((unsigned)((P.nx + TX - 1) / TX), (unsigned)((P.ny + TY - 1) / TY));
     k_flux_fused<NS><<<grid, NTHR, smem, s>>>(*reinterpret_cast<const CUtensorMap*>(tmap), L, P, Uin, Uold, Uout,
-                                              h / L.dx, h / L.dy, first_order, cell_base, st);
+                                              h / L.dx, h / L.dy, hdev, first_order, cell_base, st);
     ++*launches;
     return cudaGetLastError();
 }
 cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
-                              const double* Uold, double* Uout, double h, int first_order, int64_t cell_base,
-                              DevStatus* st, cudaStream_t s, int64_t* launches) {
-    return ns == 9 ? flux_fused_impl<9>(L, P, tmap, Uin, Uold, Uout, h, first_order, cell_base, st, s, launches)
-                   : flux_fused_impl<10>(L, P, tmap, Uin, Uold, Uout, h, first_order, cell_base, st, s, launches);
+                              const double* Uold, double* Uout, double h, const double* hdev, int first_order,
+                              int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches) {
+    return ns == 9 ? flux_fused_impl<9>(L, P, tmap, Uin, Uold, Uout, h, hdev, first_order, cell_base, st, s, launches)
+                   : flux_fused_impl<10>(L, P, tmap, Uin, Uold, Uout, h, hdev, first_order, cell_base, st, s, launches);
+}
+
+// dt = cfl / (max rate of the CFL reduction); dt[1] = dt / 2 (the flow half step)
+__global__ void k_dt_from_rate(const DevStatus* __restrict__ st, double cfl, double* __restrict__ dt) {
+    double rate;
+    const unsigned long long b = st->rate_bits;
+    memcpy(&rate, &b, sizeof rate);
+    const double d = cfl / rate;
+    dt[0] = d;
+    dt[1] = 0.5 * d;
+}
+cudaError_t launch_dt_from_rate(const DevStatus* st, double cfl, double* dt, cudaStream_t s, int64_t* launches) {
+    k_dt_from_rate<<<1, 1, 0, s>>>(st, cfl, dt);
+    ++*launches;
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- combine / validate / cfl

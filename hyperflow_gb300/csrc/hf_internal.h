@@ -48,6 +48,11 @@ inline Level make_level(const hf_level& l) {
 
 // Counter updates from the host stepper (hf_abi.cu)
 void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries);
+// Counters and device time of work run outside the ABI entry points (graph-captured steps)
+void ctx_add_launches(hf_ctx* ctx, int64_t kernels, int64_t chem_cells, int64_t chem_steps);
+bool ctx_timing_enabled(const hf_ctx* ctx);
+void ctx_add_timing(hf_ctx* ctx, double flux_ms, double chem_ms, double other_ms, int64_t flux_launches,
+                    int64_t chem_launches, int64_t other_launches);
 
 // Launch wrappers (hf_flux.cu)
 cudaError_t launch_fill(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
@@ -56,9 +61,11 @@ cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int pid
                               const double* Uold, double* Uout, double* fx, double* fy, double h,
                               int first_order, int64_t cell_base, DevStatus* st, cudaStream_t s,
                               int64_t* launches);
+// hdev (nullable): read the stage length h from device memory instead of the argument
 cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
-                              const double* Uold, double* Uout, double h, int first_order,
+                              const double* Uold, double* Uout, double h, const double* hdev, int first_order,
                               int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches);
+cudaError_t launch_dt_from_rate(const DevStatus* st, double cfl, double* dt, cudaStream_t s, int64_t* launches);
 bool make_tensor_map(void* tmap, const double* base, const hf_patch& P, int nv);
 cudaError_t launch_combine(int ns, const hf_patch& P, const double* Uold, double* U, int64_t cell_base,
                            DevStatus* st, cudaStream_t s, int64_t* launches);
@@ -85,10 +92,11 @@ cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const 
                         int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                         double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
                         int64_t* launches);
+// dt_dev (nullable): read the interval from device memory instead of dt
 cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
-                                const double* dtc, double rtol, double atol, double* h_hist, int32_t* cost,
-                                int32_t* order, unsigned long long* bins, double* trial, int* fail, DevStatus* st,
-                                int sm_count, cudaStream_t s, int64_t* launches);
+                                const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,
+                                int32_t* cost, int32_t* order, unsigned long long* bins, double* trial, int* fail,
+                                DevStatus* st, int sm_count, cudaStream_t s, int64_t* launches);
 cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
                                int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
 

@@ -3,8 +3,19 @@
 // euler() first-order redo (:257-263) and react() (:271-285).  The step-start
 // state stays untouched until the step is accepted, so a failed attempt rolls back
 // by discarding the work buffers (the reference clones the state, :413, :416).
+//
+// Two ways through a step:
+//  * graph path (fused flux + batched chemistry, CFL dt): the whole Strang step -
+//    CFL reduction, dt on the device, four fused Euler stages, ordered batched
+//    chemistry, validation - is one CUDA graph.  Every phase ORs its failure flags
+//    into one status block; the host reads it once per step.  Any flag discards the
+//    step and the host-controlled path below re-runs it.
+//  * host-controlled path: the ABI calls one by one with a status read after each,
+//    first-order redo of a failed stage, rollback and dt halving up to 18 attempts.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstring>
+#include <utility>
 #include <vector>
 #include "hf_internal.h"
 
@@ -12,7 +23,7 @@ struct hf_stepper {
     hf_ctx* ctx = nullptr;
     hf_level L{};
     hf_patch P{};
-    int nv = 12;
+    int ns = 9, nv = 12;
     int chemistry = 1;
     double rtol = 1e-8, atol = 1e-15;
     int flux_form = HF_FLUX_FUSED, chem_form = HF_CHEM_PERSISTENT;
@@ -20,6 +31,24 @@ struct hf_stepper {
     int64_t* cells = nullptr;                                // valid-cell gather list
     hf_chem_history hist{nullptr, nullptr};                  // batched chemistry history
     double time = 0.0;
+    // graph path
+    int sm_count = 1;
+    hf::DevStatus* gst = nullptr;       // step status (device)
+    hf::DevStatus* gst_host = nullptr;  // pinned mirror
+    double* ddt = nullptr;              // device [dt, dt/2]
+    double* ddt_host = nullptr;         // pinned mirror
+    double* trial = nullptr;            // chemistry scratch owned by the stepper
+    int* fail = nullptr;
+    int32_t* order = nullptr;
+    unsigned long long* bins = nullptr;
+    alignas(64) unsigned char tmap[4][128];  // TMA descriptors of the four buffers
+    double* base[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};  // by which buffer holds the state
+    int64_t graph_kernels[2] = {0, 0};             // kernels in each graph
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // recorded inside the graph
+    double graph_cfl = -1.0;
+    int use_graph = 1;
+    int64_t graph_steps = 0, host_steps = 0;
 };
 
 namespace {
@@ -50,77 +79,109 @@ hf_status flow(hf_stepper* st, const double* in, double* tmp, double* out, doubl
     return stage(st, tmp, in, out, h, s);
 }
 
-}  // namespace
+int buf_index(const hf_stepper* st, const double* p) {
+    for (int k = 0; k < 4; ++k)
+        if (st->base[k] == p) return k;
+    return 0;
+}
 
-extern "C" {
-
-hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0, int chemistry, double rtol,
-                            double atol, int flux_form, int chem_form, hf_stepper** out) {
-    if (!ctx || !level || !out || level->nx <= 0 || level->ny <= 0) return HF_ERR_ARG;
-    *out = nullptr;
-    hf_stepper* st = new hf_stepper();
-    st->ctx = ctx;
-    st->L = *level;
-    st->nv = hf_nspecies(ctx) + 3;
-    st->chemistry = chemistry;
-    st->rtol = rtol;
-    st->atol = atol;
-    st->flux_form = flux_form;
-    st->chem_form = chem_form;
-    hf_patch& P = st->P;
-    P.ilo = P.jlo = 0;
-    P.nx = level->nx;
-    P.ny = level->ny;
-    P.ng = 2;
-    P.pitch = (P.nx + 2 * P.ng + 1) & ~int64_t(1);
-    P.comp_stride = (P.pitch * (P.ny + 2 * P.ng) + 31) & ~int64_t(31);
-    P.offset = 0;
-    const size_t bytes = sizeof(double) * (size_t)P.comp_stride * st->nv;
-    for (int b = 0; b < 4; ++b) {
-        if (cudaMalloc(&st->buf[b], bytes) != cudaSuccess) { hf_stepper_destroy(st); return HF_ERR_CUDA; }
-        cudaMemset(st->buf[b], 0, bytes);
-    }
+// The graph path's Strang step from S0 into S2 (T1 and X are work buffers).
+cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, double* X, double* S2, cudaStream_t s,
+                         int64_t* nl) {
+    using namespace hf;
+    const Level L = make_level(st->L);
+    const hf_patch& P = st->P;
     const int64_t nc = (int64_t)P.nx * P.ny;
-    std::vector<int64_t> idx(nc);
-    for (int64_t j = 0; j < P.ny; ++j)
-        for (int64_t i = 0; i < P.nx; ++i) idx[j * P.nx + i] = (j + P.ng) * P.pitch + (i + P.ng);
-    if (cudaMalloc(&st->cells, sizeof(int64_t) * nc) != cudaSuccess ||
-        cudaMemcpy(st->cells, idx.data(), sizeof(int64_t) * nc, cudaMemcpyHostToDevice) != cudaSuccess) {
-        hf_stepper_destroy(st);
-        return HF_ERR_CUDA;
+    cudaError_t e;
+#define HF_Q(call) \
+    if ((e = (call)) != cudaSuccess) return e
+    HF_Q(cudaMemsetAsync(st->gst, 0, sizeof(DevStatus), s));
+    HF_Q(cudaMemsetAsync(&st->gst->bad_cell, 0xff, sizeof(unsigned long long), s));
+    HF_Q(cudaEventRecordWithFlags(st->ev[0], s, cudaEventRecordExternal));  // event-record nodes: per-phase device time
+    HF_Q(launch_cfl(st->ns, L, P, S0, st->gst, s, nl));
+    HF_Q(launch_dt_from_rate(st->gst, cfl, st->ddt, s, nl));
+    const double* half = st->ddt + 1;
+    auto tm = [&](const double* b) { return (const void*)st->tmap[buf_index(st, b)]; };
+    // flow(dt/2)
+    HF_Q(launch_flux_fused(st->ns, L, P, tm(S0), S0, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, S0, X, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(cudaEventRecordWithFlags(st->ev[1], s, cudaEventRecordExternal));
+    // react(dt): work-queue head reset, then the ordered batched kernel, commit, validate
+    HF_Q(cudaMemsetAsync(&st->gst->counter, 0, sizeof(unsigned long long), s));
+    if (st->chemistry) {
+        HF_Q(launch_chem_batched(st->ns, X, P.comp_stride, st->cells, nc, 0.0, st->ddt, nullptr, st->rtol, st->atol,
+                                 st->hist.h, st->hist.cost, st->order, st->bins, st->trial, st->fail, st->gst,
+                                 st->sm_count, s, nl));
+        HF_Q(launch_chem_commit(st->ns, X, P.comp_stride, st->cells, nc, st->trial, s, nl));
+        HF_Q(launch_validate(st->ns, P, X, 0, st->gst, s, nl));
     }
-    if (cudaMalloc(&st->hist.h, sizeof(double) * nc) != cudaSuccess ||
-        cudaMalloc(&st->hist.cost, sizeof(int32_t) * nc) != cudaSuccess ||
-        cudaMemset(st->hist.h, 0, sizeof(double) * nc) != cudaSuccess ||
-        cudaMemset(st->hist.cost, 0, sizeof(int32_t) * nc) != cudaSuccess) {
-        hf_stepper_destroy(st);
-        return HF_ERR_CUDA;
+    HF_Q(cudaEventRecordWithFlags(st->ev[2], s, cudaEventRecordExternal));
+    // flow(dt/2)
+    HF_Q(launch_flux_fused(st->ns, L, P, tm(X), X, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, X, S2, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(cudaEventRecordWithFlags(st->ev[3], s, cudaEventRecordExternal));
+#undef HF_Q
+    return cudaSuccess;
+}
+
+bool graph_ready(const hf_stepper* st) {
+    return st->use_graph && st->flux_form == HF_FLUX_FUSED && (st->chem_form == HF_CHEM_PERSISTENT || !st->chemistry);
+}
+
+// One step through the graph.  Returns HF_OK with the accepted dt, HF_ERR_INADMISSIBLE
+// with *dt = the graph's dt when the step must be re-run on the host-controlled path,
+// or HF_ERR_CUDA when no graph could be made.
+hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
+    const int k = st->buf[0] == st->base[0] ? 0 : 1;
+    if (st->graph_cfl != cfl) {
+        for (auto& g : st->exec)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        st->graph_cfl = cfl;
     }
-    if (U0) {
-        for (int n = 0; n < st->nv; ++n) {
-            cudaError_t e = cudaMemcpy2D(st->buf[0] + n * P.comp_stride + P.ng * P.pitch + P.ng, P.pitch * sizeof(double),
-                                         U0 + (size_t)n * nc, P.nx * sizeof(double), P.nx * sizeof(double), P.ny,
-                                         cudaMemcpyDeviceToDevice);
-            if (e != cudaSuccess) { hf_stepper_destroy(st); return HF_ERR_CUDA; }
+    if (!st->exec[k]) {
+        cudaGraph_t g = nullptr;
+        cudaStream_t cs = nullptr;
+        if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return HF_ERR_CUDA;
+        int64_t nl = 0;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t q = enqueue_step(st, cfl, st->buf[0], st->buf[1], st->buf[2], st->buf[3], cs, &nl);
+            e = cudaStreamEndCapture(cs, &g);
+            if (q != cudaSuccess) e = q;
         }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&st->exec[k], g, 0);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess) {
+            st->use_graph = 0;  // host-controlled path from here on
+            cudaGetLastError();
+            return HF_ERR_CUDA;
+        }
+        st->graph_kernels[k] = nl;
     }
-    *out = st;
-    return HF_OK;
+    if (cudaGraphLaunch(st->exec[k], s) != cudaSuccess ||
+        cudaMemcpyAsync(st->gst_host, st->gst, sizeof(hf::DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(st->ddt_host, st->ddt, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    hf::ctx_add_launches(st->ctx, st->graph_kernels[k], st->chemistry ? (int64_t)st->P.nx * st->P.ny : 0,
+                         (int64_t)st->gst_host->steps);
+    if (hf::ctx_timing_enabled(st->ctx)) {
+        // ev0..ev1: CFL + dt + first flow; ev1..ev2: chemistry (order, kernel, commit,
+        // validate); ev2..ev3: second flow
+        float a = 0.f, b = 0.f, c = 0.f;
+        if (cudaEventElapsedTime(&a, st->ev[0], st->ev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&b, st->ev[1], st->ev[2]) == cudaSuccess &&
+            cudaEventElapsedTime(&c, st->ev[2], st->ev[3]) == cudaSuccess)
+            hf::ctx_add_timing(st->ctx, a + c, b, 0.0, 4, st->chemistry ? 1 : 0, 2);
+        else
+            (void)cudaGetLastError();  // leave no pending error for the caller's next call
+    }
+    *dt = st->ddt_host[0];
+    return st->gst_host->flags ? HF_ERR_INADMISSIBLE : HF_OK;
 }
 
-void hf_stepper_destroy(hf_stepper* st) {
-    if (!st) return;
-    for (auto b : st->buf)
-        if (b) cudaFree(b);
-    if (st->cells) cudaFree(st->cells);
-    if (st->hist.h) cudaFree(st->hist.h);
-    if (st->hist.cost) cudaFree(st->hist.cost);
-    delete st;
-}
-
-hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) {
-    if (!st || !dt) return HF_ERR_ARG;
-    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+hf_status host_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
     double h = *dt;
     if (!(h > 0)) {
         hf_status r = hf_cfl_dt(st->ctx, &st->L, &st->P, 1, st->buf[0], cfl, &h, s);
@@ -152,6 +213,7 @@ hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) 
             st->buf[3] = S0;
             st->time += h;
             *dt = h;
+            ++st->host_steps;
             return HF_OK;
         }
         if (r == HF_ERR_ARG || r == HF_ERR_CUDA || r == HF_ERR_TIMEOUT) return r;
@@ -159,6 +221,121 @@ hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) 
         h *= 0.5;  // rollback: buf[0] was never written (BlockAMR.cpp:416)
     }
     return HF_ERR_INADMISSIBLE;
+}
+
+}  // namespace
+
+extern "C" {
+
+hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0, int chemistry, double rtol,
+                            double atol, int flux_form, int chem_form, hf_stepper** out) {
+    if (!ctx || !level || !out || level->nx <= 0 || level->ny <= 0) return HF_ERR_ARG;
+    *out = nullptr;
+    hf_stepper* st = new hf_stepper();
+    st->ctx = ctx;
+    st->L = *level;
+    st->ns = hf_nspecies(ctx);
+    st->nv = st->ns + 3;
+    st->chemistry = chemistry;
+    st->rtol = rtol;
+    st->atol = atol;
+    st->flux_form = flux_form;
+    st->chem_form = chem_form;
+    hf_patch& P = st->P;
+    P.ilo = P.jlo = 0;
+    P.nx = level->nx;
+    P.ny = level->ny;
+    P.ng = 2;
+    P.pitch = (P.nx + 2 * P.ng + 1) & ~int64_t(1);
+    P.comp_stride = (P.pitch * (P.ny + 2 * P.ng) + 31) & ~int64_t(31);
+    P.offset = 0;
+    const size_t bytes = sizeof(double) * (size_t)P.comp_stride * st->nv;
+    const int64_t nc = (int64_t)P.nx * P.ny;
+    int dev = 0;
+    bool ok = cudaGetDevice(&dev) == cudaSuccess &&
+              cudaDeviceGetAttribute(&st->sm_count, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess;
+    for (int b = 0; ok && b < 4; ++b) {
+        ok = cudaMalloc(&st->buf[b], bytes) == cudaSuccess && cudaMemset(st->buf[b], 0, bytes) == cudaSuccess;
+        st->base[b] = st->buf[b];
+    }
+    ok = ok && cudaMalloc(&st->cells, sizeof(int64_t) * nc) == cudaSuccess &&
+         cudaMalloc(&st->hist.h, sizeof(double) * nc) == cudaSuccess &&
+         cudaMalloc(&st->hist.cost, sizeof(int32_t) * nc) == cudaSuccess &&
+         cudaMemset(st->hist.h, 0, sizeof(double) * nc) == cudaSuccess &&
+         cudaMemset(st->hist.cost, 0, sizeof(int32_t) * nc) == cudaSuccess &&
+         cudaMalloc(&st->gst, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMallocHost(&st->gst_host, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMalloc(&st->ddt, 2 * sizeof(double)) == cudaSuccess &&
+         cudaMallocHost(&st->ddt_host, 2 * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&st->trial, sizeof(double) * st->nv * nc) == cudaSuccess &&
+         cudaMalloc(&st->fail, sizeof(int) * nc) == cudaSuccess &&
+         cudaMalloc(&st->order, sizeof(int32_t) * nc) == cudaSuccess &&
+         cudaMalloc(&st->bins, 16 * sizeof(unsigned long long)) == cudaSuccess;
+    for (int k = 0; ok && k < 4; ++k) ok = cudaEventCreate(&st->ev[k]) == cudaSuccess;
+    if (ok) {
+        std::vector<int64_t> idx(nc);
+        for (int64_t j = 0; j < P.ny; ++j)
+            for (int64_t i = 0; i < P.nx; ++i) idx[j * P.nx + i] = (j + P.ng) * P.pitch + (i + P.ng);
+        ok = cudaMemcpy(st->cells, idx.data(), sizeof(int64_t) * nc, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (ok && flux_form == HF_FLUX_FUSED)
+        for (int b = 0; ok && b < 4; ++b) ok = hf::make_tensor_map(st->tmap[b], st->buf[b], P, st->nv);
+    if (ok && U0) {
+        for (int n = 0; ok && n < st->nv; ++n)
+            ok = cudaMemcpy2D(st->buf[0] + n * P.comp_stride + P.ng * P.pitch + P.ng, P.pitch * sizeof(double),
+                              U0 + (size_t)n * nc, P.nx * sizeof(double), P.nx * sizeof(double), P.ny,
+                              cudaMemcpyDeviceToDevice) == cudaSuccess;
+    }
+    if (!ok) {
+        hf_stepper_destroy(st);
+        return HF_ERR_CUDA;
+    }
+    *out = st;
+    return HF_OK;
+}
+
+void hf_stepper_destroy(hf_stepper* st) {
+    if (!st) return;
+    for (auto g : st->exec)
+        if (g) cudaGraphExecDestroy(g);
+    for (auto e : st->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto b : st->base)
+        if (b) cudaFree(b);
+    cudaFree(st->cells);
+    cudaFree(st->hist.h);
+    cudaFree(st->hist.cost);
+    cudaFree(st->gst);
+    cudaFreeHost(st->gst_host);
+    cudaFree(st->ddt);
+    cudaFreeHost(st->ddt_host);
+    cudaFree(st->trial);
+    cudaFree(st->fail);
+    cudaFree(st->order);
+    cudaFree(st->bins);
+    delete st;
+}
+
+hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) {
+    if (!st || !dt) return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (!(*dt > 0) && graph_ready(st)) {
+        double h = 0.0;
+        const hf_status r = graph_step(st, cfl, &h, s);
+        if (r == HF_OK) {
+            std::swap(st->buf[0], st->buf[3]);
+            st->time += h;
+            *dt = h;
+            ++st->graph_steps;
+            return HF_OK;
+        }
+        if (r == HF_ERR_INADMISSIBLE) {
+            *dt = h;  // re-run this step with host control from the untouched start state
+            return host_step(st, cfl, dt, s);
+        }
+        // no graph: host-controlled path from here on
+    }
+    return host_step(st, cfl, dt, s);
 }
 
 hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream) {
@@ -203,5 +380,14 @@ hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream) {
 }
 
 double hf_stepper_time(const hf_stepper* st) { return st ? st->time : 0.0; }
+
+void hf_stepper_stats(const hf_stepper* st, int64_t* graph_steps, int64_t* host_steps) {
+    if (graph_steps) *graph_steps = st ? st->graph_steps : 0;
+    if (host_steps) *host_steps = st ? st->host_steps : 0;
+}
+
+void hf_stepper_set_graph(hf_stepper* st, int enable) {
+    if (st) st->use_graph = enable != 0;
+}
 
 }  // extern "C"

@@ -348,3 +348,13 @@ class Stepper:
     @property
     def time(self):
         return self.ctx.lib.hf_stepper_time(self.h)
+
+    def set_graph(self, enable=True):
+        """Use (default) or bypass the CUDA-graph path of step()."""
+        self.ctx.lib.hf_stepper_set_graph(self.h, int(bool(enable)))
+
+    def stats(self):
+        """{"graph_steps": n, "host_steps": m}."""
+        g, h = ctypes.c_int64(0), ctypes.c_int64(0)
+        self.ctx.lib.hf_stepper_stats(self.h, ctypes.byref(g), ctypes.byref(h))
+        return {"graph_steps": g.value, "host_steps": h.value}

@@ -241,6 +241,13 @@ HF_EXPORT hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream);
 HF_EXPORT hf_status hf_stepper_set_host(hf_stepper* st, const double* U, void* stream);
 HF_EXPORT hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream);
 HF_EXPORT double hf_stepper_time(const hf_stepper* st);
+/* Steps taken through the captured CUDA graph (fused flux + batched chemistry + CFL dt:
+ * one graph launch and one status read per step) and through the host-controlled path
+ * (every other case, and any graph step whose status reported a failure, re-run from the
+ * untouched start state).  Extension: the reference has no device graph. */
+HF_EXPORT void hf_stepper_stats(const hf_stepper* st, int64_t* graph_steps, int64_t* host_steps);
+/* Enable (default) or disable the graph path. */
+HF_EXPORT void hf_stepper_set_graph(hf_stepper* st, int enable);
 
 #ifdef __cplusplus
 }
