@@ -5,8 +5,9 @@ C ABI of include/hyperflow_gpu.h); this package binds it with ctypes and keeps t
 reference's per-block names (see solver.py).  There is no CPU fallback.
 """
 from .solver import (ChemistryBatch, ConservativeInterp, Context, DomainError, HyperFlowError, PatchArray,  # noqa
-                     Stepper, admissible, cfl_dt, euler_stage, fill, hllc, make_level, properties, validate)
+                     PatchSet, Stepper, admissible, average_down, cfl_dt, euler_stage, fill, hllc, make_level,
+                     properties, reflux, tag_cells, totals, validate)
 
 __all__ = ["ChemistryBatch", "ConservativeInterp", "Context", "DomainError", "HyperFlowError", "PatchArray",
-           "Stepper", "admissible", "cfl_dt", "euler_stage", "fill", "hllc", "make_level", "properties",
-           "validate"]
+           "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage", "fill", "hllc",
+           "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]

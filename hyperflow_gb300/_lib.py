@@ -45,6 +45,12 @@ class ChemHistory(ctypes.Structure):
     _fields_ = [("h", _vp), ("cost", _vp)]
 
 
+class TagCriteria(ctypes.Structure):
+    _fields_ = [("pressure_tag", _d), ("temperature_tag", _d), ("fuel_rate_tag", _d), ("density_tag", _d),
+                ("chemistry", _i32), ("box_only", _i32), ("has_box", _i32), ("pad_", _i32), ("box", _d * 4),
+                ("velocity", _d * 2)]
+
+
 # (name, restype, argtypes) for every entry point of the header
 SIGNATURES = [
     ("hf_init", _i32, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -65,6 +71,13 @@ SIGNATURES = [
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_noalloc", _i32, [ctypes.c_int, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.POINTER(_i64), _vp]),
+    ("hf_totals", _i32, [_vp, ctypes.POINTER(Patch), ctypes.c_int, _vp, _vp, _d, ctypes.c_int, _dp, _vp]),
+    ("hf_average_down", _i32, [_vp, ctypes.POINTER(Patch), ctypes.c_int, _vp, ctypes.POINTER(Patch), ctypes.c_int,
+                               _vp, _vp]),
+    ("hf_reflux", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _vp, _vp,
+                         ctypes.POINTER(Patch), ctypes.c_int, _vp, _vp, _d, _vp]),
+    ("hf_tag_cells", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d,
+                            ctypes.POINTER(TagCriteria), _vp, _vp]),
     ("hf_cfl_dt", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d, _dp, _vp]),
     ("hf_validate", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp,
                            ctypes.POINTER(_i64), _vp]),

@@ -29,6 +29,9 @@ struct hf_ctx {
     // tensor-map cache for the fused flux kernel
     struct TMap { const double* base; hf_patch P; alignas(64) unsigned char map[128]; };
     std::vector<TMap> tmaps;
+    // second scratch area for the block-AMR operations (tables, cover map, partial sums)
+    void* aux = nullptr;
+    size_t aux_bytes = 0;
     // optional per-class device timing
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -212,6 +215,7 @@ void hf_destroy(hf_ctx* ctx) {
     if (ctx->st) cudaFree(ctx->st);
     if (ctx->st_host) cudaFreeHost(ctx->st_host);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->d_patches) cudaFree(ctx->d_patches);
     delete ctx;
 }
@@ -502,6 +506,135 @@ hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patche
         if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;
         return fail(ctx, HF_ERR_INADMISSIBLE, "validate: inadmissible cell");
     }
+    return HF_OK;
+}
+
+
+// ---------------------------------------------------------------- block-AMR operations
+static char* aux_scratch(hf_ctx* ctx, size_t bytes) {
+    if (bytes > ctx->aux_bytes) {
+        if (ctx->aux) cudaFree(ctx->aux);
+        ctx->aux = nullptr;
+        ctx->aux_bytes = 0;
+        if (cudaMalloc(&ctx->aux, bytes) != cudaSuccess) return nullptr;
+        ctx->aux_bytes = bytes;
+    }
+    return static_cast<char*>(ctx->aux);
+}
+static size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+hf_status hf_totals(hf_ctx* ctx, const hf_patch* patches, int npatch, const double* U, const uint8_t* leaf_mask,
+                    double cell_volume, int absolute, double* out, void* stream) {
+    if (!ctx || !patches || npatch <= 0 || !U || !out) return fail(ctx, HF_ERR_ARG, "totals: bad arguments");
+    int64_t total = 0;
+    for (int p = 0; p < npatch; ++p) {
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "totals: bad patch");
+        total += (int64_t)patches[p].nx * patches[p].ny;
+    }
+    const int nv = ctx->ns + 3;
+    const cudaStream_t s = S(stream);
+    const size_t bp = align16(sizeof(hf_patch) * npatch), bt = align16(totals_scratch_bytes(nv));
+    char* w = aux_scratch(ctx, bp + bt + sizeof(double) * 16);
+    if (!w) return fail(ctx, HF_ERR_CUDA, "totals: scratch allocation failed");
+    HF_CUDA(cudaMemcpyAsync(w, patches, sizeof(hf_patch) * npatch, cudaMemcpyHostToDevice, s));
+    double* out_dev = reinterpret_cast<double*>(w + bp + bt);
+    HF_CUDA(launch_totals(reinterpret_cast<hf_patch*>(w), npatch, total, U, leaf_mask, nv, cell_volume, absolute,
+                          w + bp, out_dev, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(cudaMemcpyAsync(out, out_dev, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+    HF_CUDA(cudaStreamSynchronize(s));
+    return HF_OK;
+}
+
+hf_status hf_average_down(hf_ctx* ctx, const hf_patch* fine, int nfine, const double* Uf, const hf_patch* coarse,
+                          int ncoarse, double* Uc, void* stream) {
+    if (!ctx || !fine || nfine <= 0 || !Uf || !coarse || ncoarse <= 0 || !Uc)
+        return fail(ctx, HF_ERR_ARG, "average_down: bad arguments");
+    for (int p = 0; p < nfine; ++p)
+        if (!patch_ok(fine[p]) || (fine[p].ilo & 1) || (fine[p].jlo & 1) || (fine[p].nx & 1) || (fine[p].ny & 1))
+            return fail(ctx, HF_ERR_ARG, "average_down: fine patches must be aligned to the ratio 2");
+    for (int p = 0; p < ncoarse; ++p)
+        if (!patch_ok(coarse[p])) return fail(ctx, HF_ERR_ARG, "average_down: bad coarse patch");
+    const cudaStream_t s = S(stream);
+    const size_t bf = align16(sizeof(hf_patch) * nfine), bc = align16(sizeof(hf_patch) * ncoarse);
+    char* w = aux_scratch(ctx, bf + bc);
+    if (!w) return fail(ctx, HF_ERR_CUDA, "average_down: scratch allocation failed");
+    HF_CUDA(cudaMemcpyAsync(w, fine, sizeof(hf_patch) * nfine, cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(w + bf, coarse, sizeof(hf_patch) * ncoarse, cudaMemcpyHostToDevice, s));
+    HF_CUDA(launch_average_down(reinterpret_cast<hf_patch*>(w), fine, nfine, Uf, reinterpret_cast<hf_patch*>(w + bf),
+                                ncoarse, Uc, ctx->ns + 3, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(cudaStreamSynchronize(s));  // the tables live in scratch until the kernel is done
+    return HF_OK;
+}
+
+hf_status hf_reflux(hf_ctx* ctx, const hf_level* coarse_level, const hf_patch* coarse, int ncoarse, double* Uc,
+                    const double* fxc, const double* fyc, const hf_patch* fine, int nfine, const double* fxf,
+                    const double* fyf, double h, void* stream) {
+    if (!ctx || !coarse_level || !level_ok(*coarse_level) || !coarse || ncoarse <= 0 || !Uc || !fxc || !fyc ||
+        !fine || nfine <= 0 || !fxf || !fyf || !(h > 0))
+        return fail(ctx, HF_ERR_ARG, "reflux: bad arguments");
+    const int nv = ctx->ns + 3;
+    std::vector<int64_t> off(2 * (ncoarse + nfine));
+    int64_t ox = 0, oy = 0;
+    for (int p = 0; p < ncoarse; ++p) {
+        const hf_patch& C = coarse[p];
+        if (!patch_ok(C) || C.ilo < 0 || C.jlo < 0 || C.ilo + C.nx > coarse_level->nx || C.jlo + C.ny > coarse_level->ny)
+            return fail(ctx, HF_ERR_ARG, "reflux: coarse patch outside the level");
+        off[p] = ox;
+        off[ncoarse + p] = oy;
+        ox += (int64_t)nv * (C.nx + 1) * C.ny;
+        oy += (int64_t)nv * C.nx * (C.ny + 1);
+    }
+    ox = oy = 0;
+    for (int p = 0; p < nfine; ++p) {
+        const hf_patch& F = fine[p];
+        if (!patch_ok(F) || (F.ilo & 1) || (F.jlo & 1) || (F.nx & 1) || (F.ny & 1) || F.ilo < 0 || F.jlo < 0 ||
+            F.ilo + F.nx > 2 * coarse_level->nx || F.jlo + F.ny > 2 * coarse_level->ny)
+            return fail(ctx, HF_ERR_ARG, "reflux: fine patches must be aligned to the ratio 2 inside the level");
+        off[2 * ncoarse + p] = ox;
+        off[2 * ncoarse + nfine + p] = oy;
+        ox += (int64_t)nv * (F.nx + 1) * F.ny;
+        oy += (int64_t)nv * F.nx * (F.ny + 1);
+    }
+    const cudaStream_t s = S(stream);
+    const size_t bc = align16(sizeof(hf_patch) * ncoarse), bf = align16(sizeof(hf_patch) * nfine);
+    const size_t bo = align16(sizeof(int64_t) * off.size());
+    const size_t bm = sizeof(int) * (size_t)coarse_level->nx * coarse_level->ny;
+    char* w = aux_scratch(ctx, bc + bf + bo + bm);
+    if (!w) return fail(ctx, HF_ERR_CUDA, "reflux: scratch allocation failed");
+    HF_CUDA(cudaMemcpyAsync(w, coarse, sizeof(hf_patch) * ncoarse, cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(w + bc, fine, sizeof(hf_patch) * nfine, cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(w + bc + bf, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, s));
+    const int64_t* o = reinterpret_cast<const int64_t*>(w + bc + bf);
+    HF_CUDA(launch_reflux(make_level(*coarse_level), reinterpret_cast<hf_patch*>(w), coarse, ncoarse, o, o + ncoarse,
+                          fxc, fyc, Uc, reinterpret_cast<hf_patch*>(w + bc), fine, nfine, o + 2 * ncoarse,
+                          o + 2 * ncoarse + nfine, fxf, fyf, reinterpret_cast<int*>(w + bc + bf + bo), h, nv, s,
+                          &ctx->cnt.kernel_launches));
+    HF_CUDA(cudaStreamSynchronize(s));  // pageable offset table and scratch stay valid until here
+    return HF_OK;
+}
+
+hf_status hf_tag_cells(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U,
+                       double time, const hf_tag_criteria* criteria, uint8_t* tags, void* stream) {
+    if (!ctx || !level || !level_ok(*level) || !patches || npatch <= 0 || !U || !criteria || !tags)
+        return fail(ctx, HF_ERR_ARG, "tag_cells: bad arguments");
+    std::vector<int64_t> off(npatch);
+    int64_t o = 0;
+    for (int p = 0; p < npatch; ++p) {
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "tag_cells: bad patch");
+        off[p] = o;
+        o += (int64_t)patches[p].nx * patches[p].ny;
+    }
+    const cudaStream_t s = S(stream);
+    const size_t bp = align16(sizeof(hf_patch) * npatch);
+    char* w = aux_scratch(ctx, bp + sizeof(int64_t) * npatch);
+    if (!w) return fail(ctx, HF_ERR_CUDA, "tag_cells: scratch allocation failed");
+    HF_CUDA(cudaMemcpyAsync(w, patches, sizeof(hf_patch) * npatch, cudaMemcpyHostToDevice, s));
+    HF_CUDA(cudaMemcpyAsync(w + bp, off.data(), sizeof(int64_t) * npatch, cudaMemcpyHostToDevice, s));
+    HF_CUDA(reset_status(ctx, s));
+    HF_CUDA(launch_tag(ctx->ns, make_level(*level), reinterpret_cast<hf_patch*>(w), patches, npatch, U, time, *criteria,
+                       tags, reinterpret_cast<int64_t*>(w + bp), ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags) return fail(ctx, HF_ERR_INADMISSIBLE, "tag_cells: inadmissible cell on a stencil");
     return HF_OK;
 }
 

@@ -1043,6 +1043,85 @@ cudaError_t launch_chem_commit(int ns, double* U, int64_t cs, const int64_t* idx
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- tagging
+// BlockAMR::ErrorEst (BlockAMR.cpp:170-200) per valid cell: tag box (optionally moving),
+// relative pressure and temperature jumps to the face neighbours, fuel consumption
+// rate -w_H2 W_H2 / rho, plus the relative density jump (extension, density_tag > 0).
+template <int NS>
+__global__ void k_tag(Level L, const hf_patch* __restrict__ patches, const double* __restrict__ U, double t,
+                      hf_tag_criteria c, uint8_t* __restrict__ tags, const int64_t* __restrict__ tag_off,
+                      DevStatus* st) {
+    constexpr int NV = NS + 3;
+    const hf_patch P = patches[blockIdx.y];
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)P.nx * P.ny) return;
+    const int li = (int)(k % P.nx), lj = (int)(k / P.nx);
+    const int i = P.ilo + li, j = P.jlo + lj;
+    const double x = L.xlo + (i + 0.5) * L.dx - c.velocity[0] * t;
+    const double y = L.ylo + (j + 0.5) * L.dy - c.velocity[1] * t;
+    bool marked = c.has_box && x >= c.box[0] && x <= c.box[1] && y >= c.box[2] && y <= c.box[3];
+    if (!c.box_only) {
+        auto load = [&](int a, int b, double* q) {
+#pragma unroll
+            for (int n = 0; n < NV; ++n)
+                q[n] = U[P.offset + (int64_t)n * P.comp_stride + (int64_t)(b + P.ng) * P.pitch + (a + P.ng)];
+        };
+        double q[NV];
+        load(li, lj, q);
+        Props p;
+        bool ok = properties<NS>(q, p, 1000.0);
+        double rho = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) rho += q[s];
+        for (int d = 0; d < 2 && ok; ++d) {
+            const int di = d == 0, dj = d == 1;
+            double ql[NV], qr[NV];
+            load(li - di, lj - dj, ql);
+            load(li + di, lj + dj, qr);
+            Props pl, pr;
+            ok = properties<NS>(ql, pl, p.T) && properties<NS>(qr, pr, p.T);
+            if (!ok) break;
+            const double jump = fmax(fabs(pl.p - p.p) / fmin(pl.p, p.p), fabs(pr.p - p.p) / fmin(pr.p, p.p));
+            const double temp = fmax(fabs(pl.T - p.T) / fmin(pl.T, p.T), fabs(pr.T - p.T) / fmin(pr.T, p.T));
+            marked = marked || jump > c.pressure_tag || temp > c.temperature_tag;
+            if (c.density_tag > 0.0) {
+                double rl = 0.0, rr = 0.0;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) { rl += ql[s]; rr += qr[s]; }
+                const double rj = fmax(fabs(rl - rho) / fmin(rl, rho), fabs(rr - rho) / fmin(rr, rho));
+                marked = marked || rj > c.density_tag;
+            }
+        }
+        if (!ok) {
+            atomicOr(&st->flags, ST_STAGE_BAD);
+            atomicMin(&st->bad_cell, (unsigned long long)(tag_off[blockIdx.y] + k));
+        } else if (c.chemistry) {
+            double C[NS], w[NS];
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                C[s] = q[s] * INVW.v[s];
+                w[s] = 0.0;
+            }
+            KinCtx<NS> kc;
+            kin_setup<NS>(p.T, C, kc);
+            all_rates<NS>(kc, C, w, std::make_index_sequence<NR>{});
+            marked = marked || -w[0] * D_MW.v[0] / rho > c.fuel_rate_tag;
+        }
+    }
+    tags[tag_off[blockIdx.y] + k] = marked ? 1 : 0;
+}
+cudaError_t launch_tag(int ns, const Level& L, const hf_patch* patches_dev, const hf_patch* patches_host, int npatch,
+                       const double* U, double time, const hf_tag_criteria& c, uint8_t* tags, const int64_t* tag_off,
+                       DevStatus* st, cudaStream_t s, int64_t* launches) {
+    int64_t mx = 1;
+    for (int p = 0; p < npatch; ++p) mx = max(mx, (int64_t)patches_host[p].nx * patches_host[p].ny);
+    dim3 grid((unsigned)((mx + 127) / 128), (unsigned)npatch);
+    if (ns == 9) k_tag<9><<<grid, 128, 0, s>>>(L, patches_dev, U, time, c, tags, tag_off, st);
+    else k_tag<10><<<grid, 128, 0, s>>>(L, patches_dev, U, time, c, tags, tag_off, st);
+    ++*launches;
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- allocation-free entry
 // Scratch of hf_chem_advance_noalloc: a file-scope device array of fixed size, so the
 // entry point allocates nothing.  Host code reaches it only through the device address

@@ -97,6 +97,23 @@ cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* id
                                 const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,
                                 int32_t* cost, int32_t* order, unsigned long long* bins, double* trial, int* fail,
                                 DevStatus* st, int sm_count, cudaStream_t s, int64_t* launches);
+cudaError_t launch_tag(int ns, const Level& L, const hf_patch* patches_dev, const hf_patch* patches_host, int npatch,
+                       const double* U, double time, const hf_tag_criteria& c, uint8_t* tags, const int64_t* tag_off,
+                       DevStatus* st, cudaStream_t s, int64_t* launches);
+
+// Block-AMR level operations (hf_amr.cu)
+size_t totals_scratch_bytes(int nv);
+cudaError_t launch_totals(const hf_patch* patches_dev, int npatch, int64_t total, const double* U, const uint8_t* mask,
+                          int nv, double vol, int absolute, void* scratch, double* out_dev, cudaStream_t s,
+                          int64_t* launches);
+cudaError_t launch_average_down(const hf_patch* fine_dev, const hf_patch* fine_host, int nfine, const double* Uf,
+                                const hf_patch* coarse_dev, int ncoarse, double* Uc, int nv, cudaStream_t s,
+                                int64_t* launches);
+cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_patch* coarse_host, int ncoarse,
+                          const int64_t* cfx_off, const int64_t* cfy_off, const double* fxc, const double* fyc,
+                          double* Uc, const hf_patch* fine_dev, const hf_patch* fine_host, int nfine,
+                          const int64_t* ffx_off, const int64_t* ffy_off, const double* fxf, const double* fyf,
+                          int* cover, double h, int nv, cudaStream_t s, int64_t* launches);
 cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
                                int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
 

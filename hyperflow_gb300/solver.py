@@ -358,3 +358,78 @@ class Stepper:
         g, h = ctypes.c_int64(0), ctypes.c_int64(0)
         self.ctx.lib.hf_stepper_stats(self.h, ctypes.byref(g), ctypes.byref(h))
         return {"graph_steps": g.value, "host_steps": h.value}
+
+
+# ------------------------------------------------------------------ block-AMR level operations
+class PatchSet:
+    """The patches (boxes) of one level in one float64 CUDA buffer, each with ng ghost
+    layers; boxes are (ilo, jlo, ihi, jhi) inclusive, in the level's index space."""
+
+    def __init__(self, nv, boxes, ng=2, device="cuda"):
+        self.nv, self.ng, self.boxes = nv, ng, [tuple(int(v) for v in b) for b in boxes]
+        arr = (L.Patch * len(self.boxes))()
+        off = 0
+        for k, (i0, j0, i1, j1) in enumerate(self.boxes):
+            p = arr[k]
+            p.ilo, p.jlo, p.nx, p.ny, p.ng = i0, j0, i1 - i0 + 1, j1 - j0 + 1, ng
+            p.pitch = (p.nx + 2 * ng + 1) // 2 * 2
+            p.comp_stride = p.pitch * (p.ny + 2 * ng)
+            p.offset = off
+            off += nv * p.comp_stride
+        self.patches = arr
+        self.data = torch.zeros(off, dtype=torch.float64, device=device)
+
+    def __len__(self):
+        return len(self.boxes)
+
+    def view(self, k):
+        """(NV, ny+2ng, pitch) view of patch k."""
+        p = self.patches[k]
+        return self.data[p.offset:p.offset + self.nv * p.comp_stride].view(self.nv, p.ny + 2 * self.ng, p.pitch)
+
+    def interior(self, k):
+        p, g = self.patches[k], self.ng
+        return self.view(k)[:, g:g + p.ny, g:g + p.nx]
+
+    def cells(self):
+        return sum(p.nx * p.ny for p in self.patches)
+
+
+def totals(ctx, pset, cell_volume, leaf_mask=None, absolute=False):
+    """BlockAMR::totals over the valid cells (leaf_mask: uint8 CUDA tensor packing the
+    patches' cells in order, or None)."""
+    out = (ctypes.c_double * pset.nv)()
+    ctx.check(ctx.lib.hf_totals(ctx.h, pset.patches, len(pset), _ptr(pset.data), _ptr(leaf_mask), float(cell_volume),
+                                int(bool(absolute)), out, _stream()), "totals")
+    return [out[n] for n in range(pset.nv)]
+
+
+def average_down(ctx, fine, coarse):
+    """Every coarse cell under a fine patch becomes the mean of its four children."""
+    ctx.check(ctx.lib.hf_average_down(ctx.h, fine.patches, len(fine), _ptr(fine.data), coarse.patches, len(coarse),
+                                      _ptr(coarse.data), _stream()), "average_down")
+
+
+def reflux(ctx, coarse_level, coarse, fxc, fyc, fine, fxf, fyf, h):
+    """FluxRegister reflux of the coarse cells next to the fine patches (face fluxes
+    packed per patch as hf_flux_update writes them)."""
+    ctx.check(ctx.lib.hf_reflux(ctx.h, ctypes.byref(coarse_level), coarse.patches, len(coarse), _ptr(coarse.data),
+                                _ptr(fxc), _ptr(fyc), fine.patches, len(fine), _ptr(fxf), _ptr(fyf), float(h),
+                                _stream()), "reflux")
+
+
+def tag_cells(ctx, level, pset, time, pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0,
+              chemistry=True, box=None, box_only=False, velocity=(0.0, 0.0)):
+    """ErrorEst (BlockAMR.cpp:170-200) tags of the valid cells (ghost layers filled)."""
+    c = L.TagCriteria()
+    c.pressure_tag, c.temperature_tag, c.fuel_rate_tag, c.density_tag = (pressure_tag, temperature_tag,
+                                                                         fuel_rate_tag, density_tag)
+    c.chemistry, c.box_only, c.has_box = int(bool(chemistry)), int(bool(box_only)), int(box is not None)
+    if box is not None:
+        for k in range(4):
+            c.box[k] = float(box[k])
+    c.velocity[0], c.velocity[1] = float(velocity[0]), float(velocity[1])
+    tags = torch.zeros(pset.cells(), dtype=torch.uint8, device=pset.data.device)
+    ctx.check(ctx.lib.hf_tag_cells(ctx.h, ctypes.byref(level), pset.patches, len(pset), _ptr(pset.data),
+                                   float(time), ctypes.byref(c), _ptr(tags), _stream()), "tag_cells")
+    return tags

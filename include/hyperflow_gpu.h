@@ -213,6 +213,51 @@ HF_EXPORT hf_status hf_chem_advance_noalloc(int nspecies, double* U, int64_t com
                                             int64_t count, double dt, const double* dt_cell, double rtol,
                                             double atol, int64_t* first_failed, void* stream);
 
+/* ---- block-AMR level operations ---- */
+/* BlockAMR::totals (BlockAMR.cpp:347-355): out[n] = sum over the valid cells of the patches
+ * (those whose leaf_mask byte is non-zero when leaf_mask is given; leaf_mask packs the
+ * patches' cells in order, row-major) of U[n] (or |U[n]| if absolute) * cell_volume.
+ * Deterministic double-double reduction (the reference sums in long double).  out: host
+ * array of NV doubles. */
+HF_EXPORT hf_status hf_totals(hf_ctx* ctx, const hf_patch* patches, int npatch, const double* U,
+                              const uint8_t* leaf_mask, double cell_volume, int absolute, double* out,
+                              void* stream);
+/* average_down (BlockAMR.cpp:157-159, AMReX average_down at ratio 2): every coarse cell
+ * under a fine patch becomes the mean of its four children.  Fine patches have even ilo,
+ * jlo, nx, ny (level index of the fine level); their coarsened boxes lie in the coarse
+ * patches. */
+HF_EXPORT hf_status hf_average_down(hf_ctx* ctx, const hf_patch* fine, int nfine, const double* Uf,
+                                    const hf_patch* coarse, int ncoarse, double* Uc, void* stream);
+/* Reflux (BlockAMR.cpp:247-255: FluxRegister CrseInit(-h dA_c), FineAdd(+h dA_f),
+ * ClearInternalBorders, Reflux(scale 1)): every uncovered coarse cell next to a fine patch
+ * has the coarse flux of the shared face replaced by the sum of the fine fluxes.
+ * coarse_level describes the coarse level (domain, dx, periodicity); fxc/fyc and fxf/fyf
+ * are the face fluxes written by hf_flux_update for the coarse and fine patches (packed
+ * per patch in patch order); h is the stage length. */
+HF_EXPORT hf_status hf_reflux(hf_ctx* ctx, const hf_level* coarse_level, const hf_patch* coarse, int ncoarse,
+                              double* Uc, const double* fxc, const double* fyc, const hf_patch* fine, int nfine,
+                              const double* fxf, const double* fyf, double h, void* stream);
+/* Tagging criteria of BlockAMR::ErrorEst (BlockAMR.cpp:170-200) and its case keys, plus a
+ * relative density-jump criterion (extension; off when density_tag <= 0). */
+typedef struct hf_tag_criteria {
+    double pressure_tag;     /* "pressure_tag" (0.08) */
+    double temperature_tag;  /* "temperature_tag" (0.08) */
+    double fuel_rate_tag;    /* "fuel_rate_tag" (50), used when chemistry != 0 */
+    double density_tag;      /* extension: max relative density jump to a neighbour */
+    int32_t chemistry;       /* "chemistry" */
+    int32_t box_only;        /* "tag_mode" == "box" */
+    int32_t has_box;         /* "tag_box" given */
+    int32_t pad_;
+    double box[4];           /* "tag_box": x0, x1, y0, y1 */
+    double velocity[2];      /* "tag_velocity" */
+} hf_tag_criteria;
+/* ErrorEst on the valid cells of the patches (ghost layers filled): tags packs the
+ * patches' cells in order (1 = tagged).  HF_ERR_INADMISSIBLE if a cell of a stencil is
+ * inadmissible (properties() throws there in the reference). */
+HF_EXPORT hf_status hf_tag_cells(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
+                                 const double* U, double time, const hf_tag_criteria* criteria, uint8_t* tags,
+                                 void* stream);
+
 /* ---- reductions ---- */
 /* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the valid cells of the patches:
  * *dt = cfl / max((|u|+a)/dx + (|v|+a)/dy).  HF_ERR_INADMISSIBLE if a cell is not. */

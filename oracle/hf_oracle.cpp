@@ -1054,4 +1054,147 @@ double or_interp_cell(const double* q, const double* xm, const double* xp, const
     return theta;
 }
 
+
+// ---------------------------------------------------------------- block-AMR operations
+// BlockAMR::totals (BlockAMR.cpp:347-355) over count AoS cells of one level: sums of
+// U (or |U|) times the cell volume in long double, cells whose mask byte is 0 skipped.
+void or_totals(const double* U, int64_t count, const unsigned char* mask, double vol, int absolute, double* out) {
+    const int nv = NV();
+    long double sum[MAXV] = {0};
+    for (int64_t c = 0; c < count; ++c) {
+        if (mask && !mask[c]) continue;
+        for (int n = 0; n < nv; ++n) {
+            const double v = U[c * nv + n];
+            sum[n] += static_cast<long double>(absolute ? std::fabs(v) : v) * vol;
+        }
+    }
+    for (int n = 0; n < nv; ++n) out[n] = static_cast<double>(sum[n]);
+}
+
+// average_down (AMReX amrex_avgdown, ratio 2, equal volumes; BlockAMR.cpp:157-159):
+// coarse = 0.25 * (sum of the four children, accumulated jref-major, iref-minor).
+// fine: (nyf, nxf, NV) AoS with nxf, nyf even; coarse: (nyf/2, nxf/2, NV).
+void or_average_down(const double* fine, int nxf, int nyf, double* coarse) {
+    const int nv = NV(), nxc = nxf / 2, nyc = nyf / 2;
+    for (int j = 0; j < nyc; ++j) for (int i = 0; i < nxc; ++i) for (int n = 0; n < nv; ++n) {
+        double c = 0.0;
+        for (int jr = 0; jr < 2; ++jr) for (int ir = 0; ir < 2; ++ir)
+            c += fine[((size_t)(2 * j + jr) * nxf + (2 * i + ir)) * nv + n];
+        coarse[((size_t)j * nxc + i) * nv + n] = 0.25 * c;
+    }
+}
+
+// Reflux (FluxRegister CrseInit(-h dy_c) / FineAdd(+h dy_f) / ClearInternalBorders /
+// Reflux(scale 1), BlockAMR.cpp:247-255) for one coarse level covering its domain.
+//   Uc: (nyc, nxc, NV) updated coarse cells; fxc: (nyc, nxc+1, NV), fyc: (nyc+1, nxc, NV)
+//   coarse face fluxes; boxes[b] = {filo, fjlo, fihi, fjhi} fine-level boxes (even
+//   lo, odd hi); fxf + xoff[b]: box b's fine x-face fluxes (nyf, nxf+1, NV), fyf +
+//   yoff[b]: (nyf+1, nxf, NV).
+// Every uncovered coarse cell gathers, in the fixed order x-lo, x-hi, y-lo, y-hi face,
+// the register h (sum_fine dA_f F_f - dA_c F_c) of each face whose neighbour cell is
+// covered by a fine box, subtracting it on its high face and adding it on its low face
+// (divided by the coarse volume).  Periodic directions wrap the neighbour.
+void or_reflux(double* Uc, int nxc, int nyc, int periodic_x, int periodic_y, const double* fxc, const double* fyc,
+               int nbox, const int* boxes, const double* fxf, const int64_t* xoff, const double* fyf,
+               const int64_t* yoff, double h, double dxc, double dyc) {
+    const int nv = NV();
+    std::vector<int> cover((size_t)nxc * nyc, -1);
+    for (int b = 0; b < nbox; ++b)
+        for (int cj = boxes[4 * b + 1] / 2; cj <= boxes[4 * b + 3] / 2; ++cj)
+            for (int ci = boxes[4 * b] / 2; ci <= boxes[4 * b + 2] / 2; ++ci) cover[(size_t)cj * nxc + ci] = b;
+    const double dxf = 0.5 * dxc, dyf = 0.5 * dyc, vol = dxc * dyc;
+    for (int j = 0; j < nyc; ++j) for (int i = 0; i < nxc; ++i) {
+        if (cover[(size_t)j * nxc + i] >= 0) continue;
+        for (int side = 0; side < 4; ++side) {
+            const int d = side / 2, hi = side % 2;  // face on the hi side of this cell?
+            int ni = i + (d == 0 ? (hi ? 1 : -1) : 0), nj = j + (d == 1 ? (hi ? 1 : -1) : 0);
+            if (ni < 0 || ni >= nxc) { if (!periodic_x) continue; ni = (ni + nxc) % nxc; }
+            if (nj < 0 || nj >= nyc) { if (!periodic_y) continue; nj = (nj + nyc) % nyc; }
+            const int b = cover[(size_t)nj * nxc + ni];
+            if (b < 0) continue;
+            const int* B = boxes + 4 * b;
+            const int nxf = B[2] - B[0] + 1, nyf = B[3] - B[1] + 1;
+            for (int n = 0; n < nv; ++n) {
+                double Fc, F1, F2, dAc, dAf;
+                if (d == 0) {
+                    // the face between this cell and (ni, nj), on the fine box's lo x side when
+                    // this cell is to its left
+                    const int cface = hi ? i + 1 : i;
+                    Fc = fxc[((size_t)j * (nxc + 1) + cface) * nv + n];
+                    const int fi = hi ? 0 : nxf;  // fine face index in the box
+                    const int fj0 = 2 * nj - B[1];
+                    F1 = fxf[xoff[b] + ((size_t)fj0 * (nxf + 1) + fi) * nv + n];
+                    F2 = fxf[xoff[b] + ((size_t)(fj0 + 1) * (nxf + 1) + fi) * nv + n];
+                    dAc = dyc;
+                    dAf = dyf;
+                } else {
+                    const int cface = hi ? j + 1 : j;
+                    Fc = fyc[((size_t)cface * nxc + i) * nv + n];
+                    const int fj = hi ? 0 : nyf;
+                    const int fi0 = 2 * ni - B[0];
+                    F1 = fyf[yoff[b] + ((size_t)fj * nxf + fi0) * nv + n];
+                    F2 = fyf[yoff[b] + ((size_t)fj * nxf + fi0 + 1) * nv + n];
+                    dAc = dxc;
+                    dAf = dxf;
+                }
+                const double reg = -h * dAc * Fc + h * dAf * (F1 + F2);
+                Uc[((size_t)j * nxc + i) * nv + n] += (hi ? -reg : reg) / vol;
+            }
+        }
+    }
+}
+
+struct or_tag_criteria {
+    double pressure_tag, temperature_tag, fuel_rate_tag, density_tag;  // density_tag <= 0: off
+    int chemistry, box_only, has_box;
+    double box[4], velocity[2];
+};
+
+// BlockAMR::ErrorEst (BlockAMR.cpp:170-200) on a ghosted one-level array (ghosts
+// filled), plus the relative density-jump criterion (extension, off when
+// density_tag <= 0).  tags: (ny, nx) bytes, 1 = tagged.  Returns 1 if a cell on a
+// criterion's stencil is inadmissible (properties() throws there), else 0.
+int or_tag(const or_grid* g, const double* Ug, double t, const or_tag_criteria* c, unsigned char* tags) {
+    const int nv = NV();
+    for (int j = 0; j < g->ny; ++j) for (int i = 0; i < g->nx; ++i) {
+        const double x = g->xlo + (i + 0.5) * g->dx - c->velocity[0] * t;
+        const double y = g->ylo + (j + 0.5) * g->dy - c->velocity[1] * t;
+        bool marked = c->has_box && x >= c->box[0] && x <= c->box[1] && y >= c->box[2] && y <= c->box[3];
+        if (!c->box_only) {
+            double q[MAXV];
+            for (int n = 0; n < nv; ++n) q[n] = atc(g, Ug, i, j, n);
+            Props p;
+            if (!properties(q, p)) return 1;
+            for (int d = 0; d < 2; ++d) {
+                const int di = d == 0, dj = d == 1;
+                double ql[MAXV], qr[MAXV];
+                for (int n = 0; n < nv; ++n) {
+                    ql[n] = atc(g, Ug, i - di, j - dj, n);
+                    qr[n] = atc(g, Ug, i + di, j + dj, n);
+                }
+                Props pl, pr;
+                if (!properties(ql, pl) || !properties(qr, pr)) return 1;
+                const double jump = std::max(std::fabs(pl.p - p.p) / std::min(pl.p, p.p),
+                                             std::fabs(pr.p - p.p) / std::min(pr.p, p.p));
+                const double temp = std::max(std::fabs(pl.T - p.T) / std::min(pl.T, p.T),
+                                             std::fabs(pr.T - p.T) / std::min(pr.T, p.T));
+                marked = marked || jump > c->pressure_tag || temp > c->temperature_tag;
+                if (c->density_tag > 0) {
+                    const double r = density(q), rl = density(ql), rr = density(qr);
+                    const double rj = std::max(std::fabs(rl - r) / std::min(rl, r), std::fabs(rr - r) / std::min(rr, r));
+                    marked = marked || rj > c->density_tag;
+                }
+            }
+            if (c->chemistry) {
+                double C[NS_MAX], w[NS_MAX];
+                const double rho = density(q);
+                for (int k = 0; k < NS; ++k) C[k] = q[k] / MW[k];
+                net_production(p.T, C, w);
+                marked = marked || -w[0] * MW[0] / rho > c->fuel_rate_tag;
+            }
+        }
+        tags[(size_t)j * g->nx + i] = marked ? 1 : 0;
+    }
+    return 0;
+}
 }  // extern "C"

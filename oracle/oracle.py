@@ -294,3 +294,73 @@ def primitive(T, p, X=None, Y=None, u=0.0, v=0.0):
     q[len(W) + 1] = rho * v
     q[len(W) + 2] = rho * (e + 0.5 * (u * u + v * v))
     return q
+
+
+# ---------------------------------------------------------------- block-AMR operations
+class TagCriteria(ctypes.Structure):
+    _fields_ = [("pressure_tag", ctypes.c_double), ("temperature_tag", ctypes.c_double),
+                ("fuel_rate_tag", ctypes.c_double), ("density_tag", ctypes.c_double),
+                ("chemistry", ctypes.c_int), ("box_only", ctypes.c_int), ("has_box", ctypes.c_int),
+                ("box", ctypes.c_double * 4), ("velocity", ctypes.c_double * 2)]
+
+
+def _amr_sigs():
+    L = lib()
+    if getattr(L, "_amr", False):
+        return L
+    L.or_totals.argtypes = [_dp, ctypes.c_int64, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _dp]
+    L.or_average_down.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
+    L.or_reflux.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_int), _dp, ctypes.POINTER(ctypes.c_int64), _dp,
+                            ctypes.POINTER(ctypes.c_int64), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    L.or_tag.restype = ctypes.c_int
+    L.or_tag.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_double, ctypes.POINTER(TagCriteria),
+                         ctypes.POINTER(ctypes.c_ubyte)]
+    L._amr = True
+    return L
+
+
+def totals(cells, vol, mask=None, absolute=False):
+    """BlockAMR.cpp:347-355 over AoS cells (n, NV); mask: (n,) bytes or None."""
+    cells = np.ascontiguousarray(cells, dtype=np.float64)
+    out = np.zeros(cells.shape[-1])
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+    _amr_sigs().or_totals(_p(cells), len(cells), None if m is None else m.ctypes.data, float(vol), int(absolute),
+                          _p(out))
+    return out
+
+
+def average_down(fine):
+    """(nyf, nxf, NV) -> (nyf/2, nxf/2, NV)."""
+    fine = np.ascontiguousarray(fine, dtype=np.float64)
+    nyf, nxf, nv = fine.shape
+    out = np.zeros((nyf // 2, nxf // 2, nv))
+    _amr_sigs().or_average_down(_p(fine), nxf, nyf, _p(out))
+    return out
+
+
+def reflux(Uc, fxc, fyc, boxes, fxf_list, fyf_list, h, dxc, dyc, periodic=(0, 0)):
+    """Uc (nyc, nxc, NV) after reflux; boxes: [(filo, fjlo, fihi, fjhi)], fine face fluxes per box."""
+    Uc = np.ascontiguousarray(Uc, dtype=np.float64).copy()
+    nyc, nxc, nv = Uc.shape
+    fx = np.concatenate([np.ascontiguousarray(a, dtype=np.float64).ravel() for a in fxf_list])
+    fy = np.concatenate([np.ascontiguousarray(a, dtype=np.float64).ravel() for a in fyf_list])
+    xo = np.cumsum([0] + [a.size for a in fxf_list[:-1]]).astype(np.int64)
+    yo = np.cumsum([0] + [a.size for a in fyf_list[:-1]]).astype(np.int64)
+    b = np.ascontiguousarray(np.array(boxes, dtype=np.int32).ravel())
+    fxc = np.ascontiguousarray(fxc, dtype=np.float64)
+    fyc = np.ascontiguousarray(fyc, dtype=np.float64)
+    _amr_sigs().or_reflux(_p(Uc), nxc, nyc, int(periodic[0]), int(periodic[1]), _p(fxc), _p(fyc), len(boxes),
+                          b.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(fx),
+                          xo.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _p(fy),
+                          yo.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), float(h), float(dxc), float(dyc))
+    return Uc
+
+
+def tag(g, Ug, t, crit):
+    """BlockAMR::ErrorEst on a ghosted level; returns ((ny, nx) uint8 tags, status)."""
+    Ug = np.ascontiguousarray(Ug, dtype=np.float64)
+    tags = np.zeros((g.ny, g.nx), dtype=np.uint8)
+    st = _amr_sigs().or_tag(ctypes.byref(g), _p(Ug), float(t), ctypes.byref(crit),
+                            tags.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+    return tags, st

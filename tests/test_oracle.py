@@ -185,3 +185,40 @@ def test_hot_band_step_runs(oracle):
     dt = oracle.cfl_dt(g, Ug, 0.5)
     out, dta, st, stats = oracle.strang_step(g, Ug, dt)
     assert st == 0 and stats.retries == 0
+
+
+def test_reflux_makes_composite_update_conservative(oracle):
+    """With arbitrary face fluxes on a periodic coarse level and two fine boxes, the
+    composite sum (uncovered coarse cells + fine cells) of a flux-divergence update is
+    conserved only once the coarse cells next to the fine boxes are refluxed."""
+    rng = np.random.default_rng(5)
+    nxc, nyc, nv = 12, 10, 12
+    dxc, dyc, h = 2e-4, 1e-4, 1e-8
+    Uc = rng.uniform(1, 2, (nyc, nxc, nv))
+    fxc = rng.normal(size=(nyc, nxc + 1, nv))
+    fxc[:, -1] = fxc[:, 0]   # periodic: the domain's two x faces are one face
+    fyc = rng.normal(size=(nyc + 1, nxc, nv))
+    fyc[-1] = fyc[0]
+    boxes = [(4, 4, 9, 9), (16, 0, 23, 3)]
+    cover = np.zeros((nyc, nxc), bool)
+    fine_old, fine_new, fxs, fys = [], [], [], []
+    for (i0, j0, i1, j1) in boxes:
+        cover[j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2] = True
+        nxf, nyf = i1 - i0 + 1, j1 - j0 + 1
+        fx = rng.normal(size=(nyf, nxf + 1, nv))
+        fy = rng.normal(size=(nyf + 1, nxf, nv))
+        uf = rng.uniform(1, 2, (nyf, nxf, nv))
+        fine_old.append(uf)
+        fine_new.append(uf - h / (dxc / 2) * (fx[:, 1:] - fx[:, :-1]) - h / (dyc / 2) * (fy[1:] - fy[:-1]))
+        fxs.append(fx)
+        fys.append(fy)
+    new_c = Uc - h / dxc * (fxc[:, 1:] - fxc[:, :-1]) - h / dyc * (fyc[1:] - fyc[:-1])
+    refl = oracle.reflux(new_c, fxc, fyc, boxes, fxs, fys, h, dxc, dyc, periodic=(1, 1))
+    vc, vf = dxc * dyc, dxc * dyc / 4
+
+    def composite(c, fs):
+        return c[~cover].sum(0) * vc + sum(f.sum((0, 1)) for f in fs) * vf
+
+    before = composite(Uc, fine_old)
+    assert np.max(np.abs(composite(new_c, fine_new) - before)) > 1e-12 * np.max(np.abs(before))
+    assert np.max(np.abs(composite(refl, fine_new) - before)) < 1e-13 * np.max(np.abs(before))
