@@ -89,6 +89,7 @@ SIGNATURES = [
     ("hf_stepper_set_host", _i32, [_vp, _vp, _vp]),
     ("hf_stepper_get_host", _i32, [_vp, _vp, _vp]),
     ("hf_stepper_time", _d, [_vp]),
+    ("hf_stepper_cfl_dt", _i32, [_vp, _d, _dp, _vp]),
     ("hf_stepper_stats", None, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     ("hf_stepper_set_graph", None, [_vp, ctypes.c_int]),
 ]

@@ -381,6 +381,11 @@ hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream) {
 
 double hf_stepper_time(const hf_stepper* st) { return st ? st->time : 0.0; }
 
+hf_status hf_stepper_cfl_dt(hf_stepper* st, double cfl, double* dt, void* stream) {
+    if (!st || !dt) return HF_ERR_ARG;
+    return hf_cfl_dt(st->ctx, &st->L, &st->P, 1, st->buf[0], cfl, dt, stream);
+}
+
 void hf_stepper_stats(const hf_stepper* st, int64_t* graph_steps, int64_t* host_steps) {
     if (graph_steps) *graph_steps = st ? st->graph_steps : 0;
     if (host_steps) *host_steps = st ? st->host_steps : 0;

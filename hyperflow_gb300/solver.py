@@ -349,6 +349,12 @@ class Stepper:
     def time(self):
         return self.ctx.lib.hf_stepper_time(self.h)
 
+    def cfl_dt(self, cfl=0.5):
+        """stableDt of the current state (BlockAMR.cpp:335-346)."""
+        d = ctypes.c_double(0.0)
+        self.ctx.check(self.ctx.lib.hf_stepper_cfl_dt(self.h, float(cfl), ctypes.byref(d), _stream()), "cfl_dt")
+        return d.value
+
     def set_graph(self, enable=True):
         """Use (default) or bypass the CUDA-graph path of step()."""
         self.ctx.lib.hf_stepper_set_graph(self.h, int(bool(enable)))

@@ -286,6 +286,8 @@ HF_EXPORT hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream);
 HF_EXPORT hf_status hf_stepper_set_host(hf_stepper* st, const double* U, void* stream);
 HF_EXPORT hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream);
 HF_EXPORT double hf_stepper_time(const hf_stepper* st);
+/* stableDt of the current state (BlockAMR.cpp:335-346). */
+HF_EXPORT hf_status hf_stepper_cfl_dt(hf_stepper* st, double cfl, double* dt, void* stream);
 /* Steps taken through the captured CUDA graph (fused flux + batched chemistry + CFL dt:
  * one graph launch and one status read per step) and through the host-controlled path
  * (every other case, and any graph step whose status reported a failure, re-run from the
