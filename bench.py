@@ -30,6 +30,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s, 2D H2 detonation FP64: batched vs plain GPU; adjoint/forward time"
+# ncu counts of k_chem_batched (profiles/launches_det2d_2048x512_bench.md): FP64 flops per
+# integrator step attempt, and DRAM bytes (read + write) per launch per cell
+FLOPS_PER_ATTEMPT = 2.15e4
+TRAFFIC_PER_CELL = None
 NX, NY = 2048, 512
 
 
@@ -49,6 +53,9 @@ def parse():
                    help="chemistry form of the headline run")
     p.add_argument("--chem-cells", type=int, default=1 << 18,
                    help="cells of the extra chemistry-only batch (0 = skip)")
+    p.add_argument("--adj-cells", type=int, default=4096,
+                   help="0D H2/air cells of the adjoint measurement (0 disables it)")
+    p.add_argument("--adj-calls", type=int, default=2000, help="chemistry calls (of 1e-7 s) per adjoint run")
     p.add_argument("--nx", type=int, default=NX)
     p.add_argument("--ny", type=int, default=NY)
     return p.parse_args()
@@ -187,7 +194,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def timed(flux, chem, steps, warmup, timing=False, clocks=None):
+    def timed(flux, chem, steps, warmup, timing=False, clocks=None, resident=False):
         st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=flux, chem=chem)
         for _ in range(warmup):
             st.step(cfl=args.cfl)
@@ -199,9 +206,14 @@ def run_ours(args):
             clocks.start()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record()
-        for _ in range(steps):
-            st.step(cfl=args.cfl)
-            flush.zero_()
+        if resident:
+            # device-resident run: graph steps back to back, no host round trip; every
+            # step reads and writes 4 state buffers of 109 MB (> 129 MB L2), no flush
+            st.run(steps, cfl=args.cfl)
+        else:
+            for _ in range(steps):
+                st.step(cfl=args.cfl)
+                flush.zero_()
         ev1.record()
         barrier()
         ms = ev0.elapsed_time(ev1)
@@ -214,7 +226,8 @@ def run_ours(args):
         return max_over_ranks(ms), ck, tm, {k: c1[k] - c0[k] for k in c1}
 
     clocks = Clocks(local)
-    ms, ck, tm, cnt = timed(args.flux, args.chem, args.steps, args.warmup, timing=True, clocks=clocks)
+    ms, ck, tm, cnt = timed(args.flux, args.chem, args.steps, args.warmup, timing=True, clocks=clocks,
+                            resident=args.flux == "fused" and args.chem == "persistent")
     value = world * cells * args.steps / (ms * 1e-3)
     plain = None
     if not args.no_plain:
@@ -244,6 +257,37 @@ def run_ours(args):
             chem_batch[form] = {"ms": cms, "cells_per_s": world * args.chem_cells / (cms * 1e-3)}
             del field
         chem_batch["batched_over_plain"] = chem_batch["plain"]["ms"] / chem_batch["batched"]["ms"]
+
+    adjoint = None
+    if args.adj_cells > 0:
+        # discrete adjoint of 0D ignition runs: d(ignition delay, peak pressure)/d ln A_r for
+        # the 21 reactions, 2000 chemistry calls of 1e-7 s, checkpoints every 50 calls;
+        # forward = the same runs without the adjoint (hf_chem_objective)
+        ctx9 = hf.Context("H2_Li", device=local)
+        Ua = torch.from_numpy(W.ignition_batch(args.adj_cells, seed=5 + rank)).cuda()
+        adjoint = {"workload": "%d 0D H2/air cells at rest, T ~ U[1000,1500] K, p ~ U[1,5] atm, phi ~ U[0.5,2]; "
+                               "%d chemistry calls of 1e-7 s; checkpoint every 50 calls" % (args.adj_cells,
+                                                                                              args.adj_calls),
+                   "parameters": "ln A_r, 21 reactions"}
+        for obj in ("ignition_delay", "peak_pressure"):
+            sa = hf.ChemSensitivity(ctx9, 1e-7, args.adj_calls, objective=obj, checkpoint_every=50)
+            sa.objective(Ua)  # warm-up (module load, scratch)
+            barrier()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            Jf = sa.objective(Ua)
+            e1.record()
+            Ja, Ga, _ = sa.adjoint(Ua)
+            e2.record()
+            barrier()
+            fms, ams = max_over_ranks(e0.elapsed_time(e1)), max_over_ranks(e1.elapsed_time(e2))
+            ok = ~torch.isnan(Jf)
+            adjoint[obj] = {"forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
+                            "cells_with_objective": int(ok.sum().item()),
+                            "objective_median": float(Jf[ok].median().item()) if ok.any() else None,
+                            "adjoint_objective_equals_forward": bool(torch.equal(Jf[ok], Ja[ok]))}
+        adjoint["adjoint_over_forward"] = adjoint["ignition_delay"]["adjoint_over_forward"]
+        del ctx9
 
     e2e = None
     if not args.no_e2e:
@@ -275,14 +319,22 @@ def run_ours(args):
     bytes_per_launch = 2 * nv * 8 * cells  # read and write every cell state once
     achieved = bytes_per_launch / (chem_ms / max(chem_n, 1) * 1e-3) / 1e9
     hbm = pk.get("hbm_gbs", 6800.0)
-    roof = {"kernel": "k_chem_persistent", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None,
+    # FP64 roof: flops per integrator step attempt counted by ncu on this kernel
+    # (DFMA x2 + DADD + DMUL thread instructions / attempts of the launch, 512 x 128
+    # case), times the attempts counted live in the timed steps, over the live time
+    fp64_peak = ctx.fp64_peak()
+    fp64_achieved = FLOPS_PER_ATTEMPT * cnt["chem_steps"] / (chem_ms * 1e-3) / 1e9
+    roof = {"kernel": "k_chem_batched", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": TRAFFIC_PER_CELL * cells if TRAFFIC_PER_CELL else None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
-            "note": "the chemistry kernel is FP64-pipe bound, not HBM bound; the HBM fraction is reported per "
-                    "the contract, the FP64 figures are in profiles/"}
+            "fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "GFLOP/s", "frac": fp64_achieved / fp64_peak,
+                     "peak_source": "measured in this run (hf_fp64_peak: independent DFMA chains on every SM)",
+                     "flops_per_attempt": FLOPS_PER_ATTEMPT},
+            "note": "the chemistry kernel is FP64-pipe bound, not HBM bound: the HBM fraction is reported per "
+                    "the contract, the fp64 object is the binding roof; traffic = ncu dram bytes per launch"}
     cpu = None
     if not args.no_cpu:
-        cb = cpu_sample(steps=2, warm=1, rows=4, nx=args.nx)
+        cb = cpu_sample(steps=4, warm=1, rows=32, nx=args.nx)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line = {
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
@@ -291,8 +343,9 @@ def run_ours(args):
         "config": {"workload": "2D H2/O2/Ar detonation %dx%d, 64-column hot band at 40 atm/3000 K, +-1%% density "
                                "perturbation, periodic y, CFL %.2f" % (args.nx, args.ny, args.cfl),
                    "cells": cells, "species": 10, "mechanism": "H2_Li + inert AR extension",
-                   "chem_tolerances": "rtol 1e-8 atol 1e-15", "form": "fused flux + persistent chemistry",
-                   "l2": "256 MB buffer written between timed steps; state buffers 109 MB each x4",
+                   "chem_tolerances": "rtol 1e-8 atol 1e-15", "form": "fused flux + batched chemistry",
+                   "l2": "headline: device-resident run, each step reads and writes 4 state buffers of 109 MB "
+                         "(inputs larger than L2), no flush; plain form: 256 MB buffer written between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": ck, "e2e": e2e, "gpu_launches": cnt["kernel_launches"],
         "breakdown_ms_per_step": {"flux": tm["flux"][0] / args.steps, "chem": tm["chem"][0] / args.steps,
@@ -300,7 +353,7 @@ def run_ours(args):
         "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
         "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
         "chem_batch_uneven": chem_batch,
-        "roofline": roof, "cpu_baseline": cpu,
+        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

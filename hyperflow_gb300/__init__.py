@@ -4,10 +4,10 @@ The compute path is libhyperflow_gpu.so (hand-written CUDA for sm_103a behind th
 C ABI of include/hyperflow_gpu.h); this package binds it with ctypes and keeps the
 reference's per-block names (see solver.py).  There is no CPU fallback.
 """
-from .solver import (ChemistryBatch, ConservativeInterp, Context, DomainError, HyperFlowError, PatchArray,  # noqa
-                     PatchSet, Stepper, admissible, average_down, cfl_dt, euler_stage, fill, hllc, make_level,
-                     properties, reflux, tag_cells, totals, validate)
+from .solver import (ChemistryBatch, ChemObjective, ChemSensitivity, ConservativeInterp, Context,  # noqa
+                     DomainError, HyperFlowError, PatchArray, PatchSet, Stepper, admissible, average_down, cfl_dt,
+                     euler_stage, fill, hllc, make_level, properties, reflux, tag_cells, totals, validate)
 
-__all__ = ["ChemistryBatch", "ConservativeInterp", "Context", "DomainError", "HyperFlowError", "PatchArray",
-           "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage", "fill", "hllc",
-           "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]
+__all__ = ["ChemistryBatch", "ChemObjective", "ChemSensitivity", "ConservativeInterp", "Context", "DomainError",
+           "HyperFlowError", "PatchArray", "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage",
+           "fill", "hllc", "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]

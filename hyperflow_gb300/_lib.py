@@ -45,6 +45,13 @@ class ChemHistory(ctypes.Structure):
     _fields_ = [("h", _vp), ("cost", _vp)]
 
 
+class AdjointOpts(ctypes.Structure):
+    _fields_ = [("objective", _i32), ("checkpoint_every", _i32), ("ignition_dT", _d), ("rtol", _d), ("atol", _d)]
+
+
+HF_OBJ_IGNITION_DELAY, HF_OBJ_PEAK_PRESSURE, HF_OBJ_FINAL_T = range(3)
+
+
 class TagCriteria(ctypes.Structure):
     _fields_ = [("pressure_tag", _d), ("temperature_tag", _d), ("fuel_rate_tag", _d), ("density_tag", _d),
                 ("chemistry", _i32), ("box_only", _i32), ("has_box", _i32), ("pad_", _i32), ("box", _d * 4),
@@ -70,6 +77,11 @@ SIGNATURES = [
                               _vp, _d, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
+    ("hf_fp64_peak", _i32, [_vp, _dp, _vp]),
+    ("hf_chem_objective", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp,
+                                 ctypes.POINTER(_i64), _vp]),
+    ("hf_chem_adjoint", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp, _vp, _vp,
+                               ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_noalloc", _i32, [ctypes.c_int, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.POINTER(_i64), _vp]),
     ("hf_totals", _i32, [_vp, ctypes.POINTER(Patch), ctypes.c_int, _vp, _vp, _d, ctypes.c_int, _dp, _vp]),
     ("hf_average_down", _i32, [_vp, ctypes.POINTER(Patch), ctypes.c_int, _vp, ctypes.POINTER(Patch), ctypes.c_int,
@@ -85,6 +97,7 @@ SIGNATURES = [
                                  ctypes.POINTER(_vp)]),
     ("hf_stepper_destroy", None, [_vp]),
     ("hf_stepper_step", _i32, [_vp, _d, _dp, _vp]),
+    ("hf_stepper_run", _i32, [_vp, _i32, _d, ctypes.POINTER(_i32), _vp]),
     ("hf_stepper_get", _i32, [_vp, _vp, _vp]),
     ("hf_stepper_set_host", _i32, [_vp, _vp, _vp]),
     ("hf_stepper_get_host", _i32, [_vp, _vp, _vp]),

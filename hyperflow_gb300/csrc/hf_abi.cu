@@ -183,6 +183,7 @@ hf_status hf_init(const char* mechanism, int device, hf_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->st, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->st_host, sizeof(DevStatus));
     if (e == cudaSuccess) e = chem_set_rate_scale(nullptr);
+    if (e == cudaSuccess) e = adjoint_set_rate_scale(nullptr);
     if (e != cudaSuccess) {
         hf_destroy(ctx);
         return HF_ERR_CUDA;
@@ -230,6 +231,7 @@ hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale) {
     if (!ctx) return HF_ERR_ARG;
     HF_CUDA(cudaSetDevice(ctx->device));
     HF_CUDA(chem_set_rate_scale(scale));
+    HF_CUDA(adjoint_set_rate_scale(scale));
     return HF_OK;
 }
 
@@ -469,6 +471,109 @@ hf_status hf_chem_advance_batched(hf_ctx* ctx, double* U, int64_t comp_stride, c
                        stream);
 }
 
+// Objective (backward = false) or objective + discrete adjoint of 0D chemistry runs.
+// The checkpoint / segment / tape scratch is taken from the stream-ordered allocator
+// for the call only, in chunks of cells that fit half the free device memory (16 GiB
+// at most).
+static hf_status chem_sensitivity(hf_ctx* ctx, const double* U0, int64_t comp_stride, int64_t count, double dt,
+                                  int32_t ncalls, const hf_adjoint_opts* o, double* J, double* dJdp, double* dJdy0,
+                                  int64_t* first_failed, void* stream, bool backward) {
+    if (first_failed) *first_failed = -1;
+    if (!ctx || !U0 || !J || !o || count < 0 || count > INT32_MAX || comp_stride < count || !(dt > 0) ||
+        !std::isfinite(dt) || ncalls < 1 || o->objective < HF_OBJ_IGNITION_DELAY || o->objective > HF_OBJ_FINAL_T ||
+        o->checkpoint_every < 1 || !(o->rtol > 0) || !(o->atol > 0) || !std::isfinite(o->ignition_dT) ||
+        (backward && !dJdp))
+        return fail(ctx, HF_ERR_ARG, "chem_adjoint: invalid batch extent, interval, options or outputs");
+    if (count == 0) return HF_OK;
+    const cudaStream_t s = S(stream);
+    const int ns = ctx->ns, nv = ns + 3;
+    AdjointArgs a{};
+    a.U0 = U0;
+    a.cs = comp_stride;
+    a.count = count;
+    a.dt = dt;
+    a.dT = o->ignition_dT;
+    a.rtol = o->rtol;
+    a.atol = o->atol;
+    a.ncalls = ncalls;
+    a.K = o->checkpoint_every < ncalls ? o->checkpoint_every : ncalls;
+    a.objective = o->objective;
+    a.cap = 5000;  // >= the accepted-step limit of one call
+    a.backward = backward ? 1 : 0;
+    a.J = J;
+    a.dJdp = dJdp;
+    a.dJdy0 = dJdy0;
+    int* failv = static_cast<int*>(scratch(ctx, sizeof(int) * (size_t)count));
+    if (!failv) return fail(ctx, HF_ERR_CUDA, "chem_adjoint: scratch allocation failed");
+    a.fail = failv;
+    a.st = ctx->st;
+    int64_t chunk = count;
+    size_t per = 0;
+    if (backward) {
+        per = adjoint_bytes_per_cell(ns, ncalls, a.K, a.cap);
+        size_t fr = 0, tot = 0;
+        HF_CUDA(cudaMemGetInfo(&fr, &tot));
+        size_t budget = fr / 2;
+        if (budget > (size_t(16) << 30)) budget = size_t(16) << 30;
+        chunk = (int64_t)(budget / per);
+        if (chunk < 1) return fail(ctx, HF_ERR_CUDA, "chem_adjoint: not enough device memory for one cell");
+        if (chunk > count) chunk = count;
+    }
+    char* w = nullptr;
+    if (backward) {
+        const size_t bytes = per * (size_t)chunk + 1024;
+        HF_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&w), bytes, s));
+        const int nck = (ncalls + a.K - 1) / a.K;
+        size_t off = 0;
+        auto take = [&](size_t b) { char* p = w + off; off += (b + 255) & ~size_t(255); return p; };
+        a.ckpt = reinterpret_cast<double*>(take(sizeof(double) * (size_t)nck * nv * chunk));
+        a.seg = reinterpret_cast<double*>(take(sizeof(double) * (size_t)(a.K + 1) * nv * chunk));
+        a.tape = reinterpret_cast<double*>(take(sizeof(double) * (size_t)a.cap * (ns + 1) * chunk));
+        a.nstep = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * (size_t)a.K * chunk));
+        a.clipm = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)a.K * chunk));
+    }
+    hf_status rc = HF_OK;
+    cudaError_t e = reset_status(ctx, s);
+    tic(ctx, 1, s);
+    const int64_t l0 = ctx->cnt.kernel_launches;
+    for (int64_t i0 = 0; e == cudaSuccess && i0 < count; i0 += chunk) {
+        a.i0 = i0;
+        a.chunk = count - i0 < chunk ? count - i0 : chunk;
+        e = launch_chem_adjoint(ns, a, s, &ctx->cnt.kernel_launches);
+    }
+    toc(ctx, s, ctx->cnt.kernel_launches - l0);
+    if (w) {
+        const cudaError_t e2 = cudaFreeAsync(w, s);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "chem_adjoint launch");
+    HF_CUDA(read_status(ctx, s));
+    ctx->cnt.chem_steps += (int64_t)ctx->st_host->steps;
+    const unsigned f = ctx->st_host->flags;
+    if (f & (ST_CHEM_FAIL | ST_MAXSTEPS)) {
+        if (first_failed) *first_failed = (int64_t)ctx->st_host->bad_cell;
+        char msg[96];
+        snprintf(msg, sizeof msg, "chemistry cell %lld: %s", (long long)ctx->st_host->bad_cell,
+                 (f & ST_MAXSTEPS) && !(f & ST_CHEM_FAIL) ? "step limit" : "integration failed");
+        rc = fail(ctx, (f & ST_CHEM_FAIL) ? HF_ERR_CHEM_FAIL : HF_ERR_MAXSTEPS, msg);
+    }
+    return rc;
+}
+
+hf_status hf_chem_objective(hf_ctx* ctx, const double* U0, int64_t comp_stride, int64_t count, double dt,
+                            int32_t ncalls, const hf_adjoint_opts* opts, double* objective, int64_t* first_failed,
+                            void* stream) {
+    return chem_sensitivity(ctx, U0, comp_stride, count, dt, ncalls, opts, objective, nullptr, nullptr, first_failed,
+                            stream, false);
+}
+
+hf_status hf_chem_adjoint(hf_ctx* ctx, const double* U0, int64_t comp_stride, int64_t count, double dt,
+                          int32_t ncalls, const hf_adjoint_opts* opts, double* objective, double* dJ_dlnA,
+                          double* dJ_dY0, int64_t* first_failed, void* stream) {
+    return chem_sensitivity(ctx, U0, comp_stride, count, dt, ncalls, opts, objective, dJ_dlnA, dJ_dY0, first_failed,
+                            stream, true);
+}
+
 hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, const double* U, double cfl,
                     double* dt, void* stream) {
     if (!ctx || !level || !patches || npatch <= 0 || !U || !dt || !(cfl > 0) || !level_ok(*level))
@@ -635,6 +740,50 @@ hf_status hf_tag_cells(hf_ctx* ctx, const hf_level* level, const hf_patch* patch
                        tags, reinterpret_cast<int64_t*>(w + bp), ctx->st, s, &ctx->cnt.kernel_launches));
     HF_CUDA(read_status(ctx, s));
     if (ctx->st_host->flags) return fail(ctx, HF_ERR_INADMISSIBLE, "tag_cells: inadmissible cell on a stencil");
+    return HF_OK;
+}
+
+// FP64 roofline probe: independent FMA chains, 8 per thread, on every SM.
+static __global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = 1e-3 * threadIdx.x + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == -1.0) out[blockIdx.x] = s;  // never true; keeps the chains live
+}
+
+hf_status hf_fp64_peak(hf_ctx* ctx, double* gflops, void* stream) {
+    if (!ctx || !gflops) return fail(ctx, HF_ERR_ARG, "fp64_peak: bad arguments");
+    const cudaStream_t s = S(stream);
+    double* out = static_cast<double*>(scratch(ctx, sizeof(double) * 4096));
+    if (!out) return fail(ctx, HF_ERR_CUDA, "fp64_peak: scratch allocation failed");
+    cudaEvent_t e0, e1;
+    HF_CUDA(cudaEventCreate(&e0));
+    HF_CUDA(cudaEventCreate(&e1));
+    const int blocks = ctx->sm_count * 8, threads = 256, iters = 8192;
+    float best = 1e30f;
+    cudaError_t e = cudaSuccess;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(e0, s);
+        k_fp64_peak<<<blocks, threads, 0, s>>>(out, iters, 0.9999999, 1e-7);
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && t < best) best = t;  // the first launch is a warm-up
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fp64_peak");
+    ctx->cnt.kernel_launches += 4;
+    *gflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
     return HF_OK;
 }
 

@@ -331,6 +331,7 @@ __global__ void __launch_bounds__(NTHR) k_flux_fused(const __grid_constant__ CUt
                                                      const double* __restrict__ hdev, int first_order,
                                                      int64_t cell_base, DevStatus* st) {
     constexpr int NV = NS + 3;
+    if (st->abort_run) return;  // an earlier step of this device-resident run failed
     if (hdev) {  // stage length from device memory (graph-captured steps)
         const double h = *hdev;
         cx = h / L.dx;
@@ -542,6 +543,7 @@ cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const v
 
 // dt = cfl / (max rate of the CFL reduction); dt[1] = dt / 2 (the flow half step)
 __global__ void k_dt_from_rate(const DevStatus* __restrict__ st, double cfl, double* __restrict__ dt) {
+    if (st->abort_run) return;
     double rate;
     const unsigned long long b = st->rate_bits;
     memcpy(&rate, &b, sizeof rate);
@@ -574,6 +576,7 @@ __global__ void k_combine(hf_patch P, const double* __restrict__ Uold, double* _
 }
 template <int NS>
 __global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cell_base, DevStatus* st) {
+    if (st->abort_run) return;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)P.nx * P.ny) return;
     const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
@@ -586,6 +589,7 @@ __global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cel
 }
 template <int NS>
 __global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStatus* st) {
+    if (st->abort_run) return;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double rate = 0.0;
     if (idx < (int64_t)P.nx * P.ny) {

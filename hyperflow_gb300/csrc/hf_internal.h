@@ -18,6 +18,11 @@ struct DevStatus {
     unsigned long long peak_bits[16];
     unsigned long long donor[16];
     unsigned long long repairs;
+    // Set when a step of a device-resident multi-step run failed; the step kernels of
+    // the later steps of that run return at entry.  Never set outside such runs (the
+    // per-step reset of the status block leaves it alone: it is the last member).
+    unsigned int abort_run;
+    unsigned int pad2;
 };
 enum : unsigned int {
     ST_STAGE_BAD = 1u,    // a stage output cell is inadmissible
@@ -88,6 +93,28 @@ cudaError_t launch_interp(int ns, const hf_patch& C, const double* Uc, const hf_
 
 // Chemistry (hf_chem.cu)
 cudaError_t chem_set_rate_scale(const double* scale);
+
+// Discrete adjoint of 0D chemistry runs (hf_adjoint.cu).  Scratch arrays are
+// [slot][component][chunk] with chunk the stride.
+struct AdjointArgs {
+    const double* U0;
+    int64_t cs, count, i0, chunk;  // input stride, total cells, first cell and cells of this launch
+    double dt, dT, rtol, atol;
+    int ncalls, K, objective, cap, backward;
+    double* ckpt;     // [ceil(ncalls/K)][NV][chunk]
+    double* seg;      // [K+1][NV][chunk]
+    double* tape;     // [cap][NS+1][chunk]
+    int32_t* nstep;   // [K][chunk]
+    uint32_t* clipm;  // [K][chunk]
+    double* J;        // [count]
+    double* dJdp;     // [NR][count]
+    double* dJdy0;    // [NS-1][count] or null
+    int* fail;        // [count]
+    DevStatus* st;
+};
+cudaError_t adjoint_set_rate_scale(const double* scale);
+size_t adjoint_bytes_per_cell(int ns, int ncalls, int K, int cap);
+cudaError_t launch_chem_adjoint(int ns, const AdjointArgs& a, cudaStream_t s, int64_t* launches);
 cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const int64_t* cell_index,
                         int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                         double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,

@@ -12,12 +12,32 @@
 //    step and the host-controlled path below re-runs it.
 //  * host-controlled path: the ABI calls one by one with a status read after each,
 //    first-order redo of a failed stage, rollback and dt halving up to 18 attempts.
+//
+// hf_stepper_run enqueues many graph steps with no host round trip between them:
+// each step's last kernel records its dt, flags, attempt count and phase timestamps
+// in a device run record and, if the step failed, raises the status block's
+// abort_run word, after which every step kernel of the later steps returns at entry
+// (so the failed step's start state - the other ping-pong buffer - stays intact).
+// The host reads the record once per batch, accepts the steps before the failure and
+// re-runs the failed one on the host-controlled path.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstring>
 #include <utility>
 #include <vector>
 #include "hf_internal.h"
+
+namespace {
+constexpr int RUN_CAP = 256;  // steps per device-resident batch
+// Device record of a batch of graph steps.
+struct RunRec {
+    unsigned int n, pad;
+    double dt[RUN_CAP];
+    unsigned int flags[RUN_CAP];
+    unsigned long long steps[RUN_CAP];   // chemistry step attempts
+    unsigned long long t[RUN_CAP][4];    // %globaltimer at the phase boundaries (ns)
+};
+}  // namespace
 
 struct hf_stepper {
     hf_ctx* ctx = nullptr;
@@ -49,6 +69,11 @@ struct hf_stepper {
     double graph_cfl = -1.0;
     int use_graph = 1;
     int64_t graph_steps = 0, host_steps = 0;
+    // device-resident runs
+    RunRec* rec = nullptr;
+    RunRec* rec_host = nullptr;
+    cudaGraphExec_t exec_run[2] = {nullptr, nullptr};
+    int64_t run_kernels[2] = {0, 0};
 };
 
 namespace {
@@ -85,9 +110,38 @@ int buf_index(const hf_stepper* st, const double* p) {
     return 0;
 }
 
-// The graph path's Strang step from S0 into S2 (T1 and X are work buffers).
+__global__ void k_run_mark(const hf::DevStatus* st, RunRec* rec, int slot) {
+    if (st->abort_run) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    const unsigned n = rec->n;
+    if (n < RUN_CAP) rec->t[n][slot] = t;
+}
+__global__ void k_run_record(hf::DevStatus* st, const double* ddt, RunRec* rec) {
+    if (st->abort_run) return;
+    const unsigned n = rec->n;
+    if (n < RUN_CAP) {
+        rec->dt[n] = ddt[0];
+        rec->flags[n] = st->flags;
+        rec->steps[n] = st->steps;
+    }
+    rec->n = n + 1;
+    if (st->flags) st->abort_run = 1;
+}
+
+// Phase boundary k of a step: an event-record node (single steps) or a timestamp in
+// the run record (device-resident runs, whose graphs are launched many times).
+cudaError_t phase_mark(hf_stepper* st, RunRec* rec, int k, cudaStream_t s, int64_t* nl) {
+    if (!rec) return cudaEventRecordWithFlags(st->ev[k], s, cudaEventRecordExternal);
+    k_run_mark<<<1, 1, 0, s>>>(st->gst, rec, k);
+    ++*nl;
+    return cudaGetLastError();
+}
+
+// The graph path's Strang step from S0 into S2 (T1 and X are work buffers); rec
+// non-null: the step of a device-resident run.
 cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, double* X, double* S2, cudaStream_t s,
-                         int64_t* nl) {
+                         int64_t* nl, RunRec* rec = nullptr) {
     using namespace hf;
     const Level L = make_level(st->L);
     const hf_patch& P = st->P;
@@ -95,9 +149,9 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     cudaError_t e;
 #define HF_Q(call) \
     if ((e = (call)) != cudaSuccess) return e
-    HF_Q(cudaMemsetAsync(st->gst, 0, sizeof(DevStatus), s));
+    HF_Q(cudaMemsetAsync(st->gst, 0, offsetof(DevStatus, abort_run), s));  // abort_run persists over a run
     HF_Q(cudaMemsetAsync(&st->gst->bad_cell, 0xff, sizeof(unsigned long long), s));
-    HF_Q(cudaEventRecordWithFlags(st->ev[0], s, cudaEventRecordExternal));  // event-record nodes: per-phase device time
+    HF_Q(phase_mark(st, rec, 0, s, nl));  // per-phase device time
     HF_Q(launch_cfl(st->ns, L, P, S0, st->gst, s, nl));
     HF_Q(launch_dt_from_rate(st->gst, cfl, st->ddt, s, nl));
     const double* half = st->ddt + 1;
@@ -105,7 +159,7 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     // flow(dt/2)
     HF_Q(launch_flux_fused(st->ns, L, P, tm(S0), S0, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
     HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, S0, X, 0.0, half, 0, 0, st->gst, s, nl));
-    HF_Q(cudaEventRecordWithFlags(st->ev[1], s, cudaEventRecordExternal));
+    HF_Q(phase_mark(st, rec, 1, s, nl));
     // react(dt): work-queue head reset, then the ordered batched kernel, commit, validate
     HF_Q(cudaMemsetAsync(&st->gst->counter, 0, sizeof(unsigned long long), s));
     if (st->chemistry) {
@@ -115,11 +169,16 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
         HF_Q(launch_chem_commit(st->ns, X, P.comp_stride, st->cells, nc, st->trial, s, nl));
         HF_Q(launch_validate(st->ns, P, X, 0, st->gst, s, nl));
     }
-    HF_Q(cudaEventRecordWithFlags(st->ev[2], s, cudaEventRecordExternal));
+    HF_Q(phase_mark(st, rec, 2, s, nl));
     // flow(dt/2)
     HF_Q(launch_flux_fused(st->ns, L, P, tm(X), X, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
     HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, X, S2, 0.0, half, 0, 0, st->gst, s, nl));
-    HF_Q(cudaEventRecordWithFlags(st->ev[3], s, cudaEventRecordExternal));
+    HF_Q(phase_mark(st, rec, 3, s, nl));
+    if (rec) {
+        k_run_record<<<1, 1, 0, s>>>(st->gst, st->ddt, rec);
+        ++*nl;
+        HF_Q(cudaGetLastError());
+    }
 #undef HF_Q
     return cudaSuccess;
 }
@@ -131,28 +190,44 @@ bool graph_ready(const hf_stepper* st) {
 // One step through the graph.  Returns HF_OK with the accepted dt, HF_ERR_INADMISSIBLE
 // with *dt = the graph's dt when the step must be re-run on the host-controlled path,
 // or HF_ERR_CUDA when no graph could be made.
+// Drops the instantiated graphs when the CFL number changes (it is baked into them).
+void graphs_for_cfl(hf_stepper* st, double cfl) {
+    if (st->graph_cfl == cfl) return;
+    for (auto& g : st->exec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto& g : st->exec_run)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    st->graph_cfl = cfl;
+}
+
+// Captures the step of parity k (k = 0: state in base[0] -> base[3]; k = 1: the
+// reverse) as a graph; rec non-null for a device-resident run.
+cudaError_t capture_step(hf_stepper* st, double cfl, int k, RunRec* rec, cudaGraphExec_t* exec, int64_t* nl) {
+    double* S0 = st->base[k ? 3 : 0];
+    double* S2 = st->base[k ? 0 : 3];
+    cudaGraph_t g = nullptr;
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    *nl = 0;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t q = enqueue_step(st, cfl, S0, st->base[1], st->base[2], S2, cs, nl, rec);
+        e = cudaStreamEndCapture(cs, &g);
+        if (q != cudaSuccess) e = q;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    return e;
+}
+
 hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
     const int k = st->buf[0] == st->base[0] ? 0 : 1;
-    if (st->graph_cfl != cfl) {
-        for (auto& g : st->exec)
-            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
-        st->graph_cfl = cfl;
-    }
+    graphs_for_cfl(st, cfl);
     if (!st->exec[k]) {
-        cudaGraph_t g = nullptr;
-        cudaStream_t cs = nullptr;
-        if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return HF_ERR_CUDA;
         int64_t nl = 0;
-        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaError_t q = enqueue_step(st, cfl, st->buf[0], st->buf[1], st->buf[2], st->buf[3], cs, &nl);
-            e = cudaStreamEndCapture(cs, &g);
-            if (q != cudaSuccess) e = q;
-        }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&st->exec[k], g, 0);
-        if (g) cudaGraphDestroy(g);
-        cudaStreamDestroy(cs);
-        if (e != cudaSuccess) {
+        if (capture_step(st, cfl, k, nullptr, &st->exec[k], &nl) != cudaSuccess) {
             st->use_graph = 0;  // host-controlled path from here on
             cudaGetLastError();
             return HF_ERR_CUDA;
@@ -223,6 +298,59 @@ hf_status host_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
     return HF_ERR_INADMISSIBLE;
 }
 
+// Up to RUN_CAP graph steps enqueued back to back, then one read of the run record.
+// Returns the number of steps taken (accepted graph steps, plus one host-controlled
+// step when a graph step failed) in *taken.
+hf_status run_batch(hf_stepper* st, int nsteps, double cfl, cudaStream_t s, int* taken) {
+    *taken = 0;
+    graphs_for_cfl(st, cfl);
+    for (int k = 0; k < 2; ++k)
+        if (!st->exec_run[k]) {
+            int64_t nl = 0;
+            if (capture_step(st, cfl, k, st->rec, &st->exec_run[k], &nl) != cudaSuccess) {
+                cudaGetLastError();
+                return HF_ERR_CUDA;
+            }
+            st->run_kernels[k] = nl;
+        }
+    const int batch = nsteps < RUN_CAP ? nsteps : RUN_CAP;
+    if (cudaMemsetAsync(&st->gst->abort_run, 0, sizeof(unsigned int), s) != cudaSuccess ||
+        cudaMemsetAsync(&st->rec->n, 0, sizeof(unsigned int), s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    int k = st->buf[0] == st->base[0] ? 0 : 1;
+    for (int i = 0; i < batch; ++i, k ^= 1)
+        if (cudaGraphLaunch(st->exec_run[k], s) != cudaSuccess) return HF_ERR_CUDA;
+    if (cudaMemcpyAsync(st->rec_host, st->rec, sizeof(RunRec), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    const RunRec& r = *st->rec_host;
+    const int n = (int)(r.n < (unsigned)batch ? r.n : (unsigned)batch);
+    const bool failed = n > 0 && r.flags[n - 1] != 0;
+    const int acc = failed ? n - 1 : n;
+    double flux_ms = 0.0, chem_ms = 0.0;
+    int64_t attempts = 0;
+    for (int i = 0; i < acc; ++i) {
+        st->time += r.dt[i];
+        attempts += (int64_t)r.steps[i];
+        flux_ms += 1e-6 * (double)((r.t[i][1] - r.t[i][0]) + (r.t[i][3] - r.t[i][2]));
+        chem_ms += 1e-6 * (double)(r.t[i][2] - r.t[i][1]);
+    }
+    const int64_t nc = (int64_t)st->P.nx * st->P.ny;
+    hf::ctx_add_launches(st->ctx, (st->run_kernels[0] + st->run_kernels[1]) / 2 * acc, st->chemistry ? nc * acc : 0,
+                         attempts);
+    if (hf::ctx_timing_enabled(st->ctx)) hf::ctx_add_timing(st->ctx, flux_ms, chem_ms, 0.0, 4 * acc, acc, 0);
+    if (acc & 1) std::swap(st->buf[0], st->buf[3]);
+    st->graph_steps += acc;
+    *taken = acc;
+    if (failed) {
+        double h = r.dt[n - 1];  // re-run the failed step with host control from its start state
+        const hf_status q = host_step(st, cfl, &h, s);
+        if (q != HF_OK) return q;
+        *taken = acc + 1;
+    }
+    return HF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -264,6 +392,9 @@ hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0
          cudaMemset(st->hist.h, 0, sizeof(double) * nc) == cudaSuccess &&
          cudaMemset(st->hist.cost, 0, sizeof(int32_t) * nc) == cudaSuccess &&
          cudaMalloc(&st->gst, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMemset(st->gst, 0, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMalloc(&st->rec, sizeof(RunRec)) == cudaSuccess &&
+         cudaMallocHost(&st->rec_host, sizeof(RunRec)) == cudaSuccess &&
          cudaMallocHost(&st->gst_host, sizeof(hf::DevStatus)) == cudaSuccess &&
          cudaMalloc(&st->ddt, 2 * sizeof(double)) == cudaSuccess &&
          cudaMallocHost(&st->ddt_host, 2 * sizeof(double)) == cudaSuccess &&
@@ -298,6 +429,8 @@ void hf_stepper_destroy(hf_stepper* st) {
     if (!st) return;
     for (auto g : st->exec)
         if (g) cudaGraphExecDestroy(g);
+    for (auto g : st->exec_run)
+        if (g) cudaGraphExecDestroy(g);
     for (auto e : st->ev)
         if (e) cudaEventDestroy(e);
     for (auto b : st->base)
@@ -307,6 +440,8 @@ void hf_stepper_destroy(hf_stepper* st) {
     cudaFree(st->hist.cost);
     cudaFree(st->gst);
     cudaFreeHost(st->gst_host);
+    cudaFree(st->rec);
+    cudaFreeHost(st->rec_host);
     cudaFree(st->ddt);
     cudaFreeHost(st->ddt_host);
     cudaFree(st->trial);
@@ -336,6 +471,32 @@ hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) 
         // no graph: host-controlled path from here on
     }
     return host_step(st, cfl, dt, s);
+}
+
+hf_status hf_stepper_run(hf_stepper* st, int32_t nsteps, double cfl, int32_t* steps_done, void* stream) {
+    if (steps_done) *steps_done = 0;
+    if (!st || nsteps < 0 || !(cfl > 0)) return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int done = 0;
+    while (done < nsteps) {
+        int taken = 0;
+        hf_status r = HF_OK;
+        if (graph_ready(st)) {
+            r = run_batch(st, nsteps - done, cfl, s, &taken);
+            if (r == HF_ERR_CUDA && taken == 0 && st->use_graph) {
+                st->use_graph = 0;  // no run graphs: host-controlled steps from here on
+                r = HF_OK;
+            }
+        } else {
+            double h = 0.0;
+            r = hf_stepper_step(st, cfl, &h, stream);
+            taken = r == HF_OK ? 1 : 0;
+        }
+        done += taken;
+        if (steps_done) *steps_done = done;
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
 }
 
 hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream) {

@@ -97,6 +97,12 @@ class Context:
         self.lib.hf_get_timing(self.h, ms, n)
         return {k: (ms[i], n[i]) for i, k in enumerate(("flux", "chem", "other"))}
 
+    def fp64_peak(self):
+        """Measured FP64 FMA throughput of the device in GFLOP/s (hf_fp64_peak)."""
+        g = ctypes.c_double(0.0)
+        self.check(self.lib.hf_fp64_peak(self.h, ctypes.byref(g), _stream()), "fp64_peak")
+        return g.value
+
     def set_rate_scale(self, scale=None):
         if scale is None:
             self.check(self.lib.hf_set_rate_scale(self.h, None))
@@ -292,6 +298,100 @@ class ChemistryBatch:
         return field
 
 
+# ------------------------------------------------------------------ sensitivities
+OBJECTIVES = {"ignition_delay": L.HF_OBJ_IGNITION_DELAY, "peak_pressure": L.HF_OBJ_PEAK_PRESSURE,
+              "final_T": L.HF_OBJ_FINAL_T}
+
+
+class ChemSensitivity:
+    """0D constant-(rho, e) runs of `ncalls` chemistry calls of `dt` each and the
+    discrete adjoint of their objective (hf_chem_objective / hf_chem_adjoint; an
+    extension, the reference has no sensitivity code).
+
+    objective: "ignition_delay" (time T first reaches T_0 + ignition_dT, linear in t
+    between call boundaries; NaN if never), "peak_pressure" (max over boundaries) or
+    "final_T".  Gradients are d J / d ln(multiplier_r) for the 21 reactions of H2_Li,
+    the derivative of the run with its accepted step sequence frozen."""
+
+    def __init__(self, ctx, dt, ncalls, objective="ignition_delay", ignition_dT=400.0, checkpoint_every=50,
+                 rtol=1e-8, atol=1e-15):
+        if objective not in OBJECTIVES:
+            raise ValueError("unknown objective %r" % objective)
+        self.ctx = ctx
+        self.dt, self.ncalls = float(dt), int(ncalls)
+        self.opts = L.AdjointOpts(OBJECTIVES[objective], int(checkpoint_every), float(ignition_dT), float(rtol),
+                                  float(atol))
+
+    def _fail(self, st, first):
+        if st in (L.HF_ERR_CHEM_FAIL, L.HF_ERR_MAXSTEPS):
+            e = RuntimeError("chemistry cell %d: %s" % (first.value,
+                                                        (self.ctx.lib.hf_last_error(self.ctx.h) or b"").decode()))
+            e.first_failed = first.value
+            e.status = st
+            raise e
+        self.ctx.check(st, "chem_sensitivity")
+
+    def objective(self, U0):
+        """U0: (NV, n) float64 CUDA tensor (not modified) -> objective (n,)."""
+        _need_cuda64(U0, "U0")
+        U0 = U0.contiguous()
+        n = U0.shape[1]
+        J = torch.empty(n, dtype=torch.float64, device=U0.device)
+        first = ctypes.c_int64(-1)
+        st = self.ctx.lib.hf_chem_objective(self.ctx.h, _ptr(U0), n, n, self.dt, self.ncalls, ctypes.byref(self.opts),
+                                            _ptr(J), ctypes.byref(first), _stream())
+        self._fail(st, first)
+        return J
+
+    def adjoint(self, U0, initial=False):
+        """-> (J (n,), dJ/d ln multiplier (21, n), dJ/dY0 (NS-1, n) or None)."""
+        _need_cuda64(U0, "U0")
+        U0 = U0.contiguous()
+        n = U0.shape[1]
+        J = torch.empty(n, dtype=torch.float64, device=U0.device)
+        G = torch.empty(21, n, dtype=torch.float64, device=U0.device)
+        G0 = torch.empty(U0.shape[0] - 4, n, dtype=torch.float64, device=U0.device) if initial else None
+        first = ctypes.c_int64(-1)
+        st = self.ctx.lib.hf_chem_adjoint(self.ctx.h, _ptr(U0), n, n, self.dt, self.ncalls, ctypes.byref(self.opts),
+                                          _ptr(J), _ptr(G), _ptr(G0), ctypes.byref(first), _stream())
+        self._fail(st, first)
+        return J, G, G0
+
+
+class ChemObjective(torch.autograd.Function):
+    """J(ln multipliers) of a ChemSensitivity run, differentiable in the 21 log rate
+    multipliers through the discrete adjoint:
+
+        J = ChemObjective.apply(ln_mult, U0, sens);  J.sum().backward()
+
+    ln_mult: (21,) float64 tensor.  Cells whose objective is NaN (no ignition)
+    contribute nothing to the gradient.  The context's rate multipliers are reset to 1
+    after each call."""
+
+    @staticmethod
+    def forward(fctx, ln_mult, U0, sens):
+        sens.ctx.set_rate_scale(torch.exp(ln_mult.detach().double()).cpu().tolist())
+        try:
+            J = sens.objective(U0)
+        finally:
+            sens.ctx.set_rate_scale(None)
+        fctx.sens = sens
+        fctx.save_for_backward(ln_mult, U0)
+        return J
+
+    @staticmethod
+    def backward(fctx, gJ):
+        ln_mult, U0 = fctx.saved_tensors
+        sens = fctx.sens
+        sens.ctx.set_rate_scale(torch.exp(ln_mult.detach().double()).cpu().tolist())
+        try:
+            _, G, _ = sens.adjoint(U0)
+        finally:
+            sens.ctx.set_rate_scale(None)
+        g = (torch.nan_to_num(G, nan=0.0) * torch.nan_to_num(gJ, nan=0.0)[None, :]).sum(1)
+        return g.to(ln_mult.device, ln_mult.dtype), None, None
+
+
 # ------------------------------------------------------------------ stepper
 class Stepper:
     """Strang-split reacting-Euler stepper on a uniform one-patch level.
@@ -331,6 +431,14 @@ class Stepper:
         d = ctypes.c_double(float(dt))
         self.ctx.check(self.ctx.lib.hf_stepper_step(self.h, float(cfl), ctypes.byref(d), _stream()), "step")
         return d.value
+
+    def run(self, nsteps, cfl=0.5):
+        """nsteps CFL steps with no host round trip between graph steps (hf_stepper_run);
+        returns the steps completed.  Same results as nsteps calls of step()."""
+        done = ctypes.c_int32(0)
+        self.ctx.check(self.ctx.lib.hf_stepper_run(self.h, int(nsteps), float(cfl), ctypes.byref(done), _stream()),
+                       "stepper_run")
+        return done.value
 
     def state(self):
         out = torch.empty(self.nv, self.ny, self.nx, dtype=torch.float64, device="cuda")

@@ -9,6 +9,9 @@
            right.
   chem   : 2^20 independent cells, T ~ U[800, 2500] K, p ~ logU[0.1, 10] atm,
            phi ~ logU[0.3, 3], diluent ~ U[0, 0.8], dt ~ logU[1e-7, 1e-6] s.
+  ignition: 4096 0D cells of H2/air (O2 : N2 = 1 : 3.76, the reference's 9 species),
+           T ~ U[1000, 1500] K, p ~ U[1, 5] atm, phi ~ U[0.5, 2], for the sensitivity
+           (adjoint) runs.
 The diluent is argon (the inert AR extension species, 10-species mechanism) unless
 diluent="N2" is asked for (9 species, the reference mechanism as is).
 """
@@ -71,6 +74,13 @@ def chem_batch(n=1 << 20, seed=0, diluent="AR"):
     if ns == 9:
         # air-like nitrogen when the diluent is nitrogen: keep at least 3.76 N2 per O2 mole
         pass
+    return _cells_at_rest(T, p, X, ns), dt
+
+
+def _cells_at_rest(T, p, X, ns):
+    """(NV, n) conserved states at rest from temperatures, pressures and mole fractions."""
+    W = M.MW[:ns]
+    n = len(T)
     Y = X * W / (X * W).sum(1, keepdims=True)
     rho = p / (M.GAS_CONSTANT * T * (Y / W).sum(1))
     e = np.empty(n)
@@ -82,4 +92,17 @@ def chem_batch(n=1 << 20, seed=0, diluent="AR"):
     U = np.zeros((ns + 3, n))
     U[:ns] = (rho[:, None] * Y).T
     U[ns + 2] = rho * e
-    return U, dt
+    return U
+
+
+def ignition_batch(n=4096, seed=0):
+    """(NV, n) H2/air 0D cells (9 species): T ~ U[1000,1500] K, p ~ U[1,5] atm, phi ~ U[0.5,2]."""
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(1000.0, 1500.0, n)
+    p = 101325.0 * rng.uniform(1.0, 5.0, n)
+    phi = rng.uniform(0.5, 2.0, n)
+    X = np.zeros((n, 9))
+    X[:, M.SPECIES.index("H2")] = 2.0 * phi
+    X[:, M.SPECIES.index("O2")] = 1.0
+    X[:, M.SPECIES.index("N2")] = 3.76
+    return _cells_at_rest(T, p, X, 9)

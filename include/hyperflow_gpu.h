@@ -115,6 +115,11 @@ HF_EXPORT void hf_get_timing(const hf_ctx* ctx, double ms[3], int64_t launches[3
  * Used for d/d ln A_k sensitivity checks; not in the reference. */
 HF_EXPORT hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale);
 
+/* Measured FP64 FMA throughput of the device (GFLOP/s, FMA = 2 flops): the FP64 roofline
+ * denominator of the chemistry and flux kernels.  Independent FMA chains on every SM, best
+ * of three timed launches after a warm-up.  Measurement utility; no reference counterpart. */
+HF_EXPORT hf_status hf_fp64_peak(hf_ctx* ctx, double* gflops, void* stream);
+
 /* ---- EOS / flux primitives on batches (physics.cpp:4-48) ---- */
 /* properties(): q is SoA [NV][stride] device memory with count cells; writes p, a, T and
  * status[i] (0 ok, 1 inadmissible).  Returns HF_OK or HF_ERR_INADMISSIBLE if any failed. */
@@ -190,6 +195,42 @@ HF_EXPORT hf_status hf_chem_advance_batched(hf_ctx* ctx, double* U, int64_t comp
                                             int64_t count, double dt, const double* dt_cell, double rtol,
                                             double atol, const hf_chem_history* history, int64_t* first_failed,
                                             void* stream);
+
+/* Sensitivities of 0D chemistry runs (build-defined extension: the reference has no
+ * sensitivity code).  A cell at rest at constant (rho, e) is advanced by ncalls chemistry
+ * calls of dt each, every call as hf_chem_advance's plain form (Chemistry::advance,
+ * chemistry.cpp:55-76).  The objective is read at the call boundaries t_n = n dt:
+ *   HF_OBJ_IGNITION_DELAY: the time T first reaches T_0 + ignition_dT, interpolated
+ *                          linearly between the boundaries around the crossing (NaN, and
+ *                          zero gradients, when it never does);
+ *   HF_OBJ_PEAK_PRESSURE:  max_n p_n;   HF_OBJ_FINAL_T: T at t = ncalls dt. */
+enum { HF_OBJ_IGNITION_DELAY = 0, HF_OBJ_PEAK_PRESSURE = 1, HF_OBJ_FINAL_T = 2 };
+
+typedef struct hf_adjoint_opts {
+    int32_t objective;         /* HF_OBJ_* */
+    int32_t checkpoint_every;  /* chemistry calls between stored checkpoints (>= 1) */
+    double ignition_dT;        /* temperature rise that defines ignition (K) */
+    double rtol, atol;         /* integrator tolerances (the reference's: 1e-8, 1e-15) */
+} hf_adjoint_opts;
+
+/* Objective of count cells (SoA, component stride comp_stride, device memory; not
+ * modified) into objective[count] (device).  Chemistry failures: HF_ERR_CHEM_FAIL or
+ * HF_ERR_MAXSTEPS with the lowest failing cell in *first_failed, objective NaN there. */
+HF_EXPORT hf_status hf_chem_objective(hf_ctx* ctx, const double* U0, int64_t comp_stride, int64_t count, double dt,
+                                      int32_t ncalls, const hf_adjoint_opts* opts, double* objective,
+                                      int64_t* first_failed, void* stream);
+
+/* Objective and its discrete adjoint: dJ_dlnA[r*count + i] = dJ_i / d ln(multiplier_r)
+ * for the NR = 21 reactions of H2_Li.yaml in file order (duplicates separately; the
+ * multiplier scales the forward and reverse rate constants, both falloff limits), and
+ * (optional, may be NULL) dJ_dY0[k*count + i] = dJ_i / dY_k(0), k < NS-1, at fixed rho
+ * and e with the last species closing the mass.  The derivative is that of the run with
+ * its accepted step sequence frozen.  State is checkpointed every checkpoint_every calls
+ * and recomputed in the reverse sweep; the scratch (about 0.4 MB per cell for 2000 calls,
+ * 50 per checkpoint) is processed in chunks of cells.  Errors as hf_chem_objective. */
+HF_EXPORT hf_status hf_chem_adjoint(hf_ctx* ctx, const double* U0, int64_t comp_stride, int64_t count, double dt,
+                                    int32_t ncalls, const hf_adjoint_opts* opts, double* objective, double* dJ_dlnA,
+                                    double* dJ_dY0, int64_t* first_failed, void* stream);
 
 /* Chemistry without any device allocation.  No counterpart in the reference.
  *
@@ -280,6 +321,15 @@ HF_EXPORT void hf_stepper_destroy(hf_stepper* st);
 /* One Strang step.  *dt in: requested interval (<= 0: CFL dt with the given cfl);
  * out: the accepted interval. */
 HF_EXPORT hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream);
+/* nsteps CFL Strang steps with no host round trip between them (the loop of BlockAMR::run,
+ * BlockAMR.cpp:409-419, for nsteps iterations): the captured step graphs are launched back
+ * to back, up to 256 per batch, and the host reads one device record per batch.  A step
+ * whose graph raises a flag stops the batch on the device (the steps after it do nothing)
+ * and is re-run with host control (first-order redo, rollback, dt halving) exactly as
+ * hf_stepper_step would.  Same results as nsteps calls of hf_stepper_step with *dt = 0.
+ * *steps_done (may be NULL) receives the steps completed, also on error.  Other forms
+ * than fused flux + batched chemistry run hf_stepper_step nsteps times. */
+HF_EXPORT hf_status hf_stepper_run(hf_stepper* st, int32_t nsteps, double cfl, int32_t* steps_done, void* stream);
 /* Copy the valid cells out, SoA [NV][ny][nx], to DEVICE memory. */
 HF_EXPORT hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream);
 /* Copy valid cells in from / out to HOST memory (pinned or pageable), SoA [NV][ny][nx]. */

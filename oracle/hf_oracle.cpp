@@ -208,6 +208,13 @@ double troe_F(const Reaction& rx, double T, double Pr, double* dlnF_dlnPr = null
     return std::pow(10.0, lF);
 }
 
+// Rate multipliers (sensitivity parameters p_r = ln multiplier_r): reaction r's
+// forward rate constant, and with it the reverse one, is scaled by multiplier_r;
+// for falloff reactions both limits are scaled, so Pr is unchanged.  Per thread,
+// so finite-difference runs of different cells can perturb different reactions.
+thread_local const double* tl_rate_mult = nullptr;
+inline double rate_mult(int r) { return tl_rate_mult ? tl_rate_mult[r] : 1.0; }
+
 // Rates of progress (kmol/m^3/s) at T and molar concentrations C.
 void progress(double T, const double* C, Rates& out) {
     double g[NS_MAX];
@@ -217,9 +224,9 @@ void progress(double T, const double* C, Rates& out) {
         const Reaction& rx = RXN[r];
         double M = 0;
         if (rx.type != RXN_ELEMENTARY) for (int k = 0; k < NS; ++k) M += rx.eff[k] * C[k];
-        double k = rx.A * std::exp(rx.b * lnT - rx.EaR / T);
+        double k = rx.A * rate_mult(r) * std::exp(rx.b * lnT - rx.EaR / T);
         if (rx.type == RXN_FALLOFF) {
-            const double k0 = rx.A0 * std::exp(rx.b0 * lnT - rx.Ea0R / T);
+            const double k0 = rx.A0 * rate_mult(r) * std::exp(rx.b0 * lnT - rx.Ea0R / T);
             const double Pr = k0 * M / k;
             k = k * (Pr / (1 + Pr)) * troe_F(rx, T, Pr);
         } else if (rx.type == RXN_THREE_BODY) {
@@ -324,7 +331,7 @@ bool chem_jac(ChemCell& c, const double* y, double* J) {
         for (int m = 0; m < NS; ++m) dqdC[r][m] = 0;
         double M = 0;
         if (rx.type != RXN_ELEMENTARY) for (int k = 0; k < NS; ++k) M += rx.eff[k] * C[k];
-        const double kinf = rx.A * std::exp(rx.b * lnT - rx.EaR / T);
+        const double kinf = rx.A * rate_mult(r) * std::exp(rx.b * lnT - rx.EaR / T);
         const double dlnkinf = rx.b / T + rx.EaR / (T * T);
         double k = kinf, dkdT = kinf * dlnkinf, dkdM = 0;
         if (rx.type == RXN_THREE_BODY) {
@@ -332,7 +339,7 @@ bool chem_jac(ChemCell& c, const double* y, double* J) {
             k = kinf * M;
             dkdT = dkdT * M;
         } else if (rx.type == RXN_FALLOFF) {
-            const double k0 = rx.A0 * std::exp(rx.b0 * lnT - rx.Ea0R / T);
+            const double k0 = rx.A0 * rate_mult(r) * std::exp(rx.b0 * lnT - rx.Ea0R / T);
             const double dlnk0 = rx.b0 / T + rx.Ea0R / (T * T);
             const double Pr = k0 * M / kinf;
             double dlnF_dlnPr = 0, dlnF_dT = 0;
@@ -462,10 +469,11 @@ double wrms(const double* v, const double* y0, const double* y1, int n, double r
 // the Jacobian and f(y) are formed once per accepted point and reused across
 // rejected attempts.  h0 > 0 fixes the first step (no estimate); fixed != 0 turns
 // the controller off (every step accepted, used only for order checks).
-// max_steps bounds accepted steps like CVodeSetMaxNumSteps.
+// max_steps bounds accepted steps like CVodeSetMaxNumSteps.  rec (optional)
+// receives the step size of every accepted step.
 template <class Sys>
 ChemResult rosenbrock(Sys& sys, int n, double* y, double tend, double rtol, double atol, long max_steps,
-                      double h0, int fixed) {
+                      double h0, int fixed, std::vector<double>* rec = nullptr) {
     ChemResult res{CHEM_OK, 0, 0};
     double f0[NS_MAX], J[NS_MAX * NS_MAX], Mx[NS_MAX * NS_MAX], K[RS][NS_MAX], yn[NS_MAX], fy[NS_MAX], err[NS_MAX];
     int piv[NS_MAX];
@@ -547,6 +555,7 @@ ChemResult rosenbrock(Sys& sys, int n, double* y, double tend, double rtol, doub
             double hnew = h * std::min(6.0, std::max(0.2, 0.9 / std::pow(e, 0.25)));
             if (fixed) hnew = h;
             if (e <= 1.0) {
+                if (rec) rec->push_back(h);
                 t = last ? tend : t + h;
                 for (int i = 0; i < n; ++i) y[i] = yn[i];
                 if (rejectLast) hnew = std::min(hnew, h);
@@ -605,6 +614,124 @@ int chem_advance(double* u, double dt, double rtol, double atol, long max_steps,
     for (int k = 0; k < n; ++k) s += u[k];
     u[n] = c.rho - s;
     if (!properties(u, pr, c.T)) return CHEM_FAIL;
+    return CHEM_OK;
+}
+
+// ---------------------------------------------------------------- sensitivities
+// Rodas4 along a given sequence of accepted step sizes, without error control:
+// the frozen-step map whose derivative a discrete adjoint of the accepted steps
+// computes (the same stage arithmetic as rosenbrock()'s accepted path).
+template <class Sys>
+bool rosenbrock_replay(Sys& sys, int n, double* y, const double* hs, long nh) {
+    double f0[NS_MAX], J[NS_MAX * NS_MAX], Mx[NS_MAX * NS_MAX], K[RS][NS_MAX], yn[NS_MAX], fy[NS_MAX];
+    int piv[NS_MAX];
+    for (long st = 0; st < nh; ++st) {
+        const double h = hs[st];
+        if (!sys.rhs(y, f0) || !sys.jac(y, J)) return false;
+        const double inv = 1.0 / (h * RGAMMA);
+        for (int i = 0; i < n * n; ++i) Mx[i] = -J[i];
+        for (int i = 0; i < n; ++i) Mx[i * n + i] += inv;
+        if (!lu_factor(Mx, piv, n)) return false;
+        for (int s = 0; s < RS; ++s) {
+            const int base = s * (s - 1) / 2;
+            if (s == 0) {
+                for (int i = 0; i < n; ++i) fy[i] = f0[i];
+            } else {
+                for (int i = 0; i < n; ++i) yn[i] = y[i];
+                for (int j = 0; j < s; ++j) for (int i = 0; i < n; ++i) yn[i] += RA[base + j] * K[j][i];
+                if (!sys.rhs(yn, fy)) return false;
+            }
+            for (int i = 0; i < n; ++i) K[s][i] = fy[i];
+            for (int j = 0; j < s; ++j) {
+                const double cc = RC[base + j] / h;
+                for (int i = 0; i < n; ++i) K[s][i] += cc * K[j][i];
+            }
+            lu_solve(Mx, piv, K[s], n);
+        }
+        for (int i = 0; i < n; ++i) {
+            double v = y[i];
+            for (int s = 0; s < RS; ++s) v += RM[s] * K[s][i];
+            if (!std::isfinite(v)) return false;
+            y[i] = v;
+        }
+    }
+    return true;
+}
+
+// One chemistry call (chemistry.cpp:55-76) on AoS cell u, recording the accepted
+// step sizes into rec, or (hs != null) replaying nh given steps.
+int chem_substep(double* u, double dt, double rtol, double atol, std::vector<double>* rec, const double* hs,
+                 long nh) {
+    if (!(dt > 0) || !std::isfinite(dt)) return CHEM_FAIL;
+    Props pr;
+    if (!properties(u, pr, 1000.0)) return CHEM_FAIL;
+    ChemCell c;
+    c.rho = density(u);
+    c.e = internal_energy(u);
+    c.T = pr.T;
+    const int n = NS - 1;
+    double y[NS_MAX];
+    for (int k = 0; k < n; ++k) y[k] = u[k] / c.rho;
+    ChemSys sys{c};
+    if (hs) {
+        if (!rosenbrock_replay(sys, n, y, hs, nh)) return CHEM_FAIL;
+    } else {
+        const ChemResult r = rosenbrock(sys, n, y, dt, rtol, atol, 5000, 0.0, 0, rec);
+        if (r.status != CHEM_OK) return r.status;
+    }
+    double s = 0;
+    for (int k = 0; k < n; ++k) {
+        if (!std::isfinite(y[k]) || y[k] < -1e-13) return CHEM_FAIL;
+        u[k] = c.rho * std::max(0., y[k]);
+    }
+    for (int k = 0; k < n; ++k) s += u[k];
+    u[n] = c.rho - s;
+    if (!properties(u, pr, c.T)) return CHEM_FAIL;
+    return CHEM_OK;
+}
+
+// Objectives of a 0D constant-(rho, e) run of nsub chemistry calls of dt each,
+// from T_n and p_n at the call boundaries t_n = n dt (build-defined: the
+// reference has no sensitivity code):
+//   ignition delay: the time T first reaches T_0 + dT, interpolated linearly in t
+//     between the two boundaries around the crossing (NaN if it never does);
+//   peak pressure: max_n p_n;  final temperature: T_nsub.
+enum { OBJ_IGNITION = 0, OBJ_PEAK_PRESSURE = 1, OBJ_FINAL_T = 2 };
+
+double objective_value(int obj, const std::vector<double>& T, const std::vector<double>& p, double dt, double dT) {
+    if (obj == OBJ_FINAL_T) return T.back();
+    if (obj == OBJ_PEAK_PRESSURE) return *std::max_element(p.begin(), p.end());
+    const double Ts = T[0] + dT;
+    for (size_t n = 0; n + 1 < T.size(); ++n)
+        if (T[n + 1] >= Ts) return n * dt + dt * (Ts - T[n]) / (T[n + 1] - T[n]);
+    return std::numeric_limits<double>::quiet_NaN();
+}
+
+// Runs one cell; rec/counts record the accepted steps of every call, or hs/hcounts
+// replay them.  Returns a CHEM_* status.
+int cell_objective(const double* u0, double dt, int nsub, int obj, double dT, double rtol, double atol,
+                   std::vector<double>* rec, std::vector<long>* counts, const double* hs, const long* hcounts,
+                   double* J) {
+    const int nv = NV();
+    double u[MAXV];
+    std::copy(u0, u0 + nv, u);
+    std::vector<double> T, p;
+    Props pr;
+    if (!properties(u, pr, 1000.0)) return CHEM_FAIL;
+    T.push_back(pr.T);
+    p.push_back(pr.p);
+    long off = 0;
+    for (int n = 0; n < nsub; ++n) {
+        const size_t before = rec ? rec->size() : 0;
+        const int st = chem_substep(u, dt, rtol, atol, rec, hs ? hs + off : nullptr, hs ? hcounts[n] : 0);
+        if (st != CHEM_OK) return st;
+        if (rec && counts) counts->push_back((long)(rec->size() - before));
+        if (hs) off += hcounts[n];
+        if (!properties(u, pr, T.back())) return CHEM_FAIL;
+        T.push_back(pr.T);
+        p.push_back(pr.p);
+    }
+    *J = objective_value(obj, T, p, dt, dT);
     return CHEM_OK;
 }
 
@@ -745,6 +872,67 @@ int64_t or_chem_batch(double* U, int64_t count, double dt, const double* dt_cell
     if (steps_out) for (int64_t k = 0; k < count; ++k) steps_out[k] = steps[k];
     for (int64_t k = 0; k < count; ++k) if (fail[k]) return k;
     std::copy(trial.begin(), trial.end(), U);
+    return -1;
+}
+
+// Objective (OBJ_*) of count AoS cells over nsub adaptive chemistry calls of dt
+// each; mult: NR rate multipliers (null = 1).  Returns -1, or the lowest failing cell.
+int64_t or_chem_objective(const double* U0, int64_t count, double dt, int nsub, int obj, double dT, double rtol,
+                          double atol, const double* mult, int threads, double* J) {
+    const int nv = NV();
+    std::vector<int> fail(count, 0);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < count; ++k) {
+        tl_rate_mult = mult;
+        fail[k] = cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, nullptr, nullptr, nullptr, nullptr, &J[k]);
+        tl_rate_mult = nullptr;
+    }
+    for (int64_t k = 0; k < count; ++k) if (fail[k]) return k;
+    return -1;
+}
+
+// Central differences of the objective in p_r = ln multiplier_r, r = 0..NR-1,
+// step fd_h, into grad[k*NR + r]; J[k] is the unperturbed objective.  frozen != 0
+// replays each cell's accepted step sequence of the unperturbed run (the map a
+// discrete adjoint differentiates); frozen == 0 re-runs the adaptive integrator.
+int64_t or_chem_sens_fd(const double* U0, int64_t count, double dt, int nsub, int obj, double dT, double rtol,
+                        double atol, double fd_h, int frozen, int threads, double* J, double* grad) {
+    const int nv = NV();
+    std::vector<int> fail(count, 0);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < count; ++k) {
+        double mult[NR];
+        for (int r = 0; r < NR; ++r) mult[r] = 1.0;
+        tl_rate_mult = mult;
+        std::vector<double> rec;
+        std::vector<long> counts;
+        int st = cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, &rec, &counts, nullptr, nullptr, &J[k]);
+        for (int r = 0; st == CHEM_OK && r < NR; ++r) {
+            double Jp = 0, Jm = 0;
+            mult[r] = std::exp(fd_h);
+            st = frozen ? cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, nullptr, nullptr, rec.data(),
+                                         counts.data(), &Jp)
+                        : cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, nullptr, nullptr, nullptr,
+                                         nullptr, &Jp);
+            mult[r] = std::exp(-fd_h);
+            if (st == CHEM_OK)
+                st = frozen ? cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, nullptr, nullptr, rec.data(),
+                                             counts.data(), &Jm)
+                            : cell_objective(&U0[k * nv], dt, nsub, obj, dT, rtol, atol, nullptr, nullptr, nullptr,
+                                             nullptr, &Jm);
+            mult[r] = 1.0;
+            grad[k * NR + r] = (Jp - Jm) / (2 * fd_h);
+        }
+        tl_rate_mult = nullptr;
+        fail[k] = st;
+    }
+    for (int64_t k = 0; k < count; ++k) if (fail[k]) return k;
     return -1;
 }
 

@@ -66,6 +66,13 @@ def lib():
         L.or_chem_batch.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int, _lp]
         L.or_rodas4_circle.argtypes = [_dp, ctypes.c_double, ctypes.c_int]
+        L.or_chem_objective.restype = ctypes.c_int64
+        L.or_chem_objective.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_int, _dp]
+        L.or_chem_sens_fd.restype = ctypes.c_int64
+        L.or_chem_sens_fd.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_int, _dp, _dp]
         L.or_fill_ghosts.argtypes = [ctypes.POINTER(Grid), _dp]
         L.or_euler_stage.argtypes = [ctypes.POINTER(Grid), _dp, _dp, ctypes.c_double, ctypes.c_int, _dp, _dp]
         L.or_repair_roundoff.argtypes = [ctypes.POINTER(Grid), _dp, _lp]
@@ -191,6 +198,31 @@ def chem_batch(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
     bad = lib().or_chem_batch(_p(U), len(U), float(dt), None if dtc is None else _p(dtc), float(rtol),
                               float(atol), int(threads), steps.ctypes.data_as(_lp))
     return U, int(bad), steps
+
+
+OBJECTIVES = {"ignition_delay": 0, "peak_pressure": 1, "final_T": 2}
+
+
+def chem_objective(U, dt, nsub, objective, dT=400.0, rtol=1e-8, atol=1e-15, mult=None, threads=0):
+    """Objective of AoS 0D cells over nsub adaptive chemistry calls of dt each;
+    mult: rate multipliers (NR) or None.  Returns (J, first_failed or -1)."""
+    U = np.ascontiguousarray(np.array(U, dtype=np.float64).reshape(-1, nspecies() + 3))
+    J = np.zeros(len(U))
+    m = None if mult is None else np.ascontiguousarray(mult, dtype=np.float64)
+    bad = lib().or_chem_objective(_p(U), len(U), float(dt), int(nsub), OBJECTIVES[objective], float(dT),
+                                  float(rtol), float(atol), None if m is None else _p(m), int(threads), _p(J))
+    return J, int(bad)
+
+
+def chem_sens_fd(U, dt, nsub, objective, dT=400.0, rtol=1e-8, atol=1e-15, fd_h=1e-6, frozen=True, threads=0):
+    """Central differences dJ/d(ln multiplier_r) (count, NR); frozen replays the
+    unperturbed accepted step sequence.  Returns (J, grad, first_failed or -1)."""
+    U = np.ascontiguousarray(np.array(U, dtype=np.float64).reshape(-1, nspecies() + 3))
+    J = np.zeros(len(U))
+    G = np.zeros((len(U), 21))
+    bad = lib().or_chem_sens_fd(_p(U), len(U), float(dt), int(nsub), OBJECTIVES[objective], float(dT), float(rtol),
+                                float(atol), float(fd_h), int(bool(frozen)), int(threads), _p(J), _p(G))
+    return J, G, int(bad)
 
 
 def rodas4_circle(y, tend, nsteps):

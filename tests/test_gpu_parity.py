@@ -357,3 +357,27 @@ def test_graph_step_equals_host_step(gpu):
     assert a.stats()["graph_steps"] == 3 and b.stats()["graph_steps"] == 0
     assert torch.equal(a.state(), b.state())
     assert a.time == b.time
+
+
+@pytest.mark.parametrize("cfl", [0.5, 2.5])
+def test_device_resident_run_equals_steps(gpu, cfl):
+    """hf_stepper_run (graph steps launched back to back, one record read per batch)
+    gives the states, times and step kinds of the same number of step() calls.  At CFL
+    2.5 graph steps fail: the run stops on the device at the failed step and re-runs it
+    with host control (rollback, dt halving), like step() does."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import workloads as W
+    U, lvd = W.det2d(seed=3, diluent="N2", nx=96, ny=24, hot_columns=8)
+    lv = hf.make_level(**lvd)
+    a = hf.Stepper(gpu, lv, cuda(U), flux="fused", chem="batched")
+    b = hf.Stepper(gpu, lv, cuda(U), flux="fused", chem="batched")
+    assert a.run(5, cfl=cfl) == 5
+    for _ in range(5):
+        b.step(cfl=cfl)
+    assert torch.equal(a.state(), b.state())
+    assert a.time == b.time
+    assert a.stats() == b.stats()
+    if cfl > 1:
+        assert a.stats()["host_steps"] > 0
+    else:
+        assert a.stats()["graph_steps"] == 5
