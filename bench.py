@@ -56,6 +56,11 @@ def parse():
     p.add_argument("--adj-cells", type=int, default=4096,
                    help="0D H2/air cells of the adjoint measurement (0 disables it)")
     p.add_argument("--adj-calls", type=int, default=2000, help="chemistry calls (of 1e-7 s) per adjoint run")
+    p.add_argument("--adj-objectives", default="ignition_delay",
+                   help="comma-separated: ignition_delay, peak_pressure, final_T")
+    p.add_argument("--adj1d-cells", type=int, default=1000,
+                   help="cells of the 1D detonation whose run is differentiated (0 disables it)")
+    p.add_argument("--adj1d-steps", type=int, default=1000, help="CFL Strang steps of that run")
     p.add_argument("--nx", type=int, default=NX)
     p.add_argument("--ny", type=int, default=NY)
     return p.parse_args()
@@ -269,7 +274,7 @@ def run_ours(args):
                                "%d chemistry calls of 1e-7 s; checkpoint every 50 calls" % (args.adj_cells,
                                                                                               args.adj_calls),
                    "parameters": "ln A_r, 21 reactions"}
-        for obj in ("ignition_delay", "peak_pressure"):
+        for obj in args.adj_objectives.split(","):
             sa = hf.ChemSensitivity(ctx9, 1e-7, args.adj_calls, objective=obj, checkpoint_every=50)
             sa.objective(Ua)  # warm-up (module load, scratch)
             barrier()
@@ -286,8 +291,48 @@ def run_ours(args):
                             "cells_with_objective": int(ok.sum().item()),
                             "objective_median": float(Jf[ok].median().item()) if ok.any() else None,
                             "adjoint_objective_equals_forward": bool(torch.equal(Jf[ok], Ja[ok]))}
-        adjoint["adjoint_over_forward"] = adjoint["ignition_delay"]["adjoint_over_forward"]
+        adjoint["adjoint_over_forward"] = max(v["adjoint_over_forward"] for v in adjoint.values()
+                                              if isinstance(v, dict))
         del ctx9
+
+    if args.adj1d_cells > 0:
+        # discrete adjoint of the 1D planar detonation (H2/O2/Ar, nx x 2 cells on 0.1 m,
+        # 20-cell driver): d(induction length)/d ln A_r and d/dU0 over adj1d_steps CFL
+        # steps with checkpoints every 50; forward = recording the run (plain forms)
+        U1, lv1 = W.det1d(diluent="AR", nx=args.adj1d_cells)
+        level1 = hf.make_level(**lv1)
+        barrier()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        t0 = time.perf_counter()
+        e0.record()
+        fa = hf.FlowAdjoint(ctx, level1, torch.from_numpy(U1).cuda(), args.adj1d_steps, cfl=args.cfl,
+                            checkpoint_every=50)
+        e1.record()
+        t1 = time.perf_counter()
+        Uf = fa.final.clone().requires_grad_(True)
+        Jl = hf.induction_length(Uf, lv1["dx"])
+        (seed,) = torch.autograd.grad(Jl, Uf)
+        t2 = time.perf_counter()
+        e2.record()  # the seed's torch ops are not part of either phase
+        ea = torch.cuda.Event(enable_timing=True)
+        _, gl = fa.adjoint(seed.contiguous())
+        ea.record()
+        barrier()
+        t3 = time.perf_counter()
+        fwd = max_over_ranks(e0.elapsed_time(e1))
+        adj = max_over_ranks(e2.elapsed_time(ea))
+        fa.close()
+        if adjoint is None:
+            adjoint = {}
+        adjoint["flow_1d"] = {
+            "workload": "1D H2/O2/Ar detonation %dx2 cells on 0.1 m, 20-cell driver at 40 atm/3000 K, %d CFL %.2f "
+                        "Strang steps, checkpoint every 50" % (args.adj1d_cells, args.adj1d_steps, args.cfl),
+            "objective": "induction length (shock-to-reaction-front distance), %.4e m" % float(Jl.item()),
+            "forward_ms": fwd, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd,
+            "host_wall_s": {"forward": t1 - t0, "adjoint": t3 - t2},
+            "dJ_dlnA_largest": [int(k) for k in np.argsort(-np.abs(gl))[:3]]}
+        adjoint["adjoint_over_forward"] = max(v["adjoint_over_forward"] for v in adjoint.values()
+                                              if isinstance(v, dict) and "adjoint_over_forward" in v)
 
     e2e = None
     if not args.no_e2e:

@@ -5,9 +5,10 @@ C ABI of include/hyperflow_gpu.h); this package binds it with ctypes and keeps t
 reference's per-block names (see solver.py).  There is no CPU fallback.
 """
 from .solver import (ChemistryBatch, ChemObjective, ChemSensitivity, ConservativeInterp, Context,  # noqa
-                     DomainError, HyperFlowError, PatchArray, PatchSet, Stepper, admissible, average_down, cfl_dt,
-                     euler_stage, fill, hllc, make_level, properties, reflux, tag_cells, totals, validate)
+                     DomainError, FlowAdjoint, HyperFlowError, PatchArray, PatchSet, Stepper, admissible,
+                     average_down, cfl_dt, euler_stage, fill, hllc, induction_length, make_level, properties, reflux,
+                     tag_cells, totals, validate)
 
 __all__ = ["ChemistryBatch", "ChemObjective", "ChemSensitivity", "ConservativeInterp", "Context", "DomainError",
-           "HyperFlowError", "PatchArray", "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage",
+           "FlowAdjoint", "HyperFlowError", "induction_length", "PatchArray", "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage",
            "fill", "hllc", "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]

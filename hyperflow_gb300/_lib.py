@@ -78,6 +78,10 @@ SIGNATURES = [
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
     ("hf_fp64_peak", _i32, [_vp, _dp, _vp]),
+    ("hf_flow_record", _i32, [_vp, ctypes.POINTER(Level), _vp, _i32, _vp, _d, _i32, ctypes.c_int, _d, _d, _vp, _vp,
+                              ctypes.POINTER(_vp), _vp]),
+    ("hf_flow_adjoint", _i32, [_vp, _vp, _vp, _vp, _vp]),
+    ("hf_flow_tape_destroy", None, [_vp]),
     ("hf_chem_objective", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp,
                                  ctypes.POINTER(_i64), _vp]),
     ("hf_chem_adjoint", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp, _vp, _vp,

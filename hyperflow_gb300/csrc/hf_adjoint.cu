@@ -328,15 +328,18 @@ __device__ __noinline__ bool chem_vjp(double rho, double e, double& T, const dou
 #pragma unroll
     for (int k = 0; k < NS; ++k) gC[k] = 0.0;
     all_vjp<NS>(kc, C, wbar, 1.0 / rho, gC, gT, wf, pbar, std::make_index_sequence<NR>{});
+    // inside the small jump of e(T) at T_mid the inversion returns T_mid, which does
+    // not move with y or e: no derivative through T there
+    const bool stuck = T == TMID;
     const double cl = rho * gC[L] * INVW.v[L];
 #pragma unroll
-    for (int j = 0; j < N; ++j) ybar[j] = rho * gC[j] * INVW.v[j] - cl + dTdy[j] * gT;
+    for (int j = 0; j < N; ++j) ybar[j] = rho * gC[j] * INVW.v[j] - cl + (stuck ? 0.0 : dTdy[j] * gT);
     if (re) {
         double zg = 0.0;
 #pragma unroll
         for (int k = 0; k < NS; ++k) zg = fma(z[k], gC[k], zg);
         re[0] += zg - wf / rho;
-        re[1] += gT / (RU * cv);
+        if (!stuck) re[1] += gT / (RU * cv);
     }
     return true;
 }
@@ -429,18 +432,22 @@ __device__ __noinline__ bool chem_hess(double rho, double e, double& T, const do
         tw = fma(dTdy[j], wT[j], tw);
         cw = fma(cvk[j] - cvk[L], wT[j], cw);
     }
+    // at the T_mid jump T(y, e) = T_mid does not move: the matrix J keeps its
+    // dT/dy formula, whose y-derivative at fixed T is the only curvature left
+    const bool stuck = T == TMID;
     const double cl = rho * gC[L] * INVW.v[L], icv = 1.0 / cv;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        const double hT = -(ETT * dTdy[j] * tw + dTdy[j] * cw + (cvk[j] - cvk[L]) * tw) * icv;
-        ybar[j] += rho * gC[j] * INVW.v[j] - cl + dTdy[j] * gT + hT;
+        const double hT = stuck ? -(cvk[j] - cvk[L]) * tw * icv
+                                : -(ETT * dTdy[j] * tw + dTdy[j] * cw + (cvk[j] - cvk[L]) * tw) * icv;
+        ybar[j] += rho * gC[j] * INVW.v[j] - cl + (stuck ? 0.0 : dTdy[j] * gT) + hT;
     }
     if (re) {
         double zg = 0.0;
 #pragma unroll
         for (int k = 0; k < NS; ++k) zg = fma(z[k], gC[k], zg);
         re[0] += zg - tw / rho;
-        re[1] += (gT - (cw + ETT * tw) * icv) * icv / RU;
+        if (!stuck) re[1] += (gT - (cw + ETT * tw) * icv) * icv / RU;
     }
     return true;
 }
@@ -624,8 +631,10 @@ namespace {
 enum { OBJ_IGNITION = HF_OBJ_IGNITION_DELAY, OBJ_PEAK_PRESSURE = HF_OBJ_PEAK_PRESSURE, OBJ_FINAL_T = HF_OBJ_FINAL_T };
 
 // Forward pass: ncalls calls with checkpoints (ckpt may be null), objective
-// bookkeeping; then (backward != 0) the reverse sweep.  One thread per cell.
-template <int NS>
+// bookkeeping; then (BACKWARD) the reverse sweep.  One thread per cell.  The
+// forward-only instantiation carries none of the reverse sweep's registers or stack.
+#pragma nv_diag_suppress 128  // the forward-only instantiation ends before the reverse sweep's loops
+template <int NS, bool BACKWARD>
 __global__ void __launch_bounds__(32) k_chem_adjoint(AdjointArgs a) {
     constexpr int N = NS - 1, NV = NS + 3;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -669,7 +678,7 @@ __global__ void __launch_bounds__(32) k_chem_adjoint(AdjointArgs a) {
                         : n_ign * a.dt + a.dt * (Ts - Ta) / (Tb - Ta);
     a.J[gi] = Jv;
     a.fail[gi] = 0;
-    if (!a.backward) return;
+    if constexpr (!BACKWARD) return;
     double pbar[NR], lam[N];
 #pragma unroll
     for (int r = 0; r < NR; ++r) pbar[r] = 0.0;
@@ -774,7 +783,109 @@ __global__ void __launch_bounds__(32) k_chem_adjoint(AdjointArgs a) {
     }
 }
 
+#pragma nv_diag_default 128
+
+// Adjoint of the react phase of a Strang step on the cells of a ghosted patch: one
+// chemistry call (plain form, the frozen accepted steps recomputed into the tape)
+// per cell.  ubar_in = (du_out/du_in)^T ubar_out through
+//   u_in -> (y = u_k/rho, rho = sum u_k, e = E/rho - |m|^2/(2 rho^2)) -> Rodas4 steps
+//   -> clip -> u_out_k = rho max(0, y_k), u_out_L = rho - sum u_out_k, m and E unchanged,
+// and pcell[r][cell] += dJ/d ln A_r of the cell.  One thread per cell of [i0, i0+chunk).
+template <int NS>
+__global__ void __launch_bounds__(32) k_chem_call_adjoint(hf_patch P, const double* __restrict__ U,
+                                                          const double* __restrict__ ubar_out,
+                                                          double* __restrict__ ubar_in, double dt, double rtol,
+                                                          double atol, double* __restrict__ tape, int cap, int64_t i0,
+                                                          int64_t chunk, double* __restrict__ pcell, DevStatus* st) {
+    constexpr int N = NS - 1, NV = NS + 3;
+    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nc = (int64_t)P.nx * P.ny, i = i0 + li;
+    if (li >= chunk || i >= nc) return;
+    const int ci = (int)(i % P.nx), cj = (int)(i / P.nx);
+    const int64_t g = P.offset + (int64_t)(cj + P.ng) * P.pitch + (ci + P.ng);
+    double u[NV], ub[NV], uc[NV];
+#pragma unroll
+    for (int n = 0; n < NV; ++n) {
+        u[n] = U[g + n * P.comp_stride];
+        ub[n] = ubar_out[g + n * P.comp_stride];
+        uc[n] = u[n];
+    }
+    int nrec = 0;
+    uint32_t clip = 0;
+    const int r = run_call<NS>(uc, dt, rtol, atol, tape + li, chunk, nrec, cap, clip);
+    double out[NV];
+#pragma unroll
+    for (int n = 0; n < NV; ++n) out[n] = 0.0;
+    bool ok = r == CELL_DONE && nrec <= cap;
+    if (ok) {
+        double rho = 0.0;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) rho += u[k];
+        const double ir = 1.0 / rho;
+        const double mx = u[NS], my = u[NS + 1], E = u[NS + 2];
+        const double e = E * ir - 0.5 * ((mx * ir) * (mx * ir) + (my * ir) * (my * ir));
+        // output side: u_out_k = rho Y'_k (k < N), u_out_L = rho (1 - sum Y'_k)
+        double lam[N], rhob = ub[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const double d = ub[k] - ub[N];
+            lam[k] = (clip >> k & 1u) ? 0.0 : rho * d;
+            rhob = fma(uc[k] * ir, d, rhob);
+        }
+        double pb[NR], re[2] = {0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < NR; ++q) pb[q] = 0.0;
+        for (int s = nrec - 1; ok && s >= 0; --s) {
+            const double* t = tape + li + (int64_t)s * (N + 2) * chunk;
+            double ys[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) ys[k] = t[k * chunk];
+            ok = step_adjoint<NS>(rho, e, t[(N + 1) * chunk], ys, t[N * chunk], lam, pb, re);
+        }
+        if (ok) {
+#pragma unroll
+            for (int q = 0; q < NR; ++q) pcell[(int64_t)q * nc + i] += pb[q];
+            // input side: y_k = u_k / rho, rho = sum u_k, e(E, m, rho)
+            rhob += re[0];
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                out[k] = lam[k] * ir;
+                rhob = fma(-lam[k] * u[k] * ir, ir, rhob);
+            }
+            const double eb = re[1];
+            out[NS + 2] = ub[NS + 2] + eb * ir;
+            out[NS] = ub[NS] - eb * mx * ir * ir;
+            out[NS + 1] = ub[NS + 1] - eb * my * ir * ir;
+            rhob += eb * (-E * ir * ir + (mx * mx + my * my) * ir * ir * ir);
+#pragma unroll
+            for (int k = 0; k < NS; ++k) out[k] += rhob;
+        }
+    }
+    if (!ok) {
+        atomicOr(&st->flags, ST_CHEM_FAIL);
+        atomicMin(&st->bad_cell, (unsigned long long)i);
+    }
+#pragma unroll
+    for (int n = 0; n < NV; ++n) ubar_in[g + n * P.comp_stride] = out[n];
+}
+
 }  // namespace
+
+cudaError_t launch_chem_call_adjoint(int ns, const hf_patch& P, const double* U, const double* ubar_out,
+                                     double* ubar_in, double dt, double rtol, double atol, double* tape, int cap,
+                                     int64_t i0, int64_t chunk, double* pcell, DevStatus* st, cudaStream_t s,
+                                     int64_t* launches) {
+    if (chunk <= 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((chunk + 31) / 32);
+    if (ns == 9)
+        k_chem_call_adjoint<9><<<grid, 32, 0, s>>>(P, U, ubar_out, ubar_in, dt, rtol, atol, tape, cap, i0, chunk, pcell,
+                                                   st);
+    else
+        k_chem_call_adjoint<10><<<grid, 32, 0, s>>>(P, U, ubar_out, ubar_in, dt, rtol, atol, tape, cap, i0, chunk,
+                                                    pcell, st);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
 
 size_t adjoint_bytes_per_cell(int ns, int ncalls, int K, int cap) {
     const int nv = ns + 3, n = ns - 1;
@@ -786,8 +897,13 @@ size_t adjoint_bytes_per_cell(int ns, int ncalls, int K, int cap) {
 cudaError_t launch_chem_adjoint(int ns, const AdjointArgs& a, cudaStream_t s, int64_t* launches) {
     if (a.chunk <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)((a.chunk + 31) / 32);
-    if (ns == 9) k_chem_adjoint<9><<<grid, 32, 0, s>>>(a);
-    else k_chem_adjoint<10><<<grid, 32, 0, s>>>(a);
+    if (a.backward) {
+        if (ns == 9) k_chem_adjoint<9, true><<<grid, 32, 0, s>>>(a);
+        else k_chem_adjoint<10, true><<<grid, 32, 0, s>>>(a);
+    } else {
+        if (ns == 9) k_chem_adjoint<9, false><<<grid, 32, 0, s>>>(a);
+        else k_chem_adjoint<10, false><<<grid, 32, 0, s>>>(a);
+    }
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -113,6 +113,20 @@ struct AdjointArgs {
     DevStatus* st;
 };
 cudaError_t adjoint_set_rate_scale(const double* scale);
+// Adjoint of one chemistry call per cell of a ghosted patch (cells [i0, i0+chunk));
+// tape: [cap][NS+1][chunk] scratch; pcell: [NR][nx*ny] accumulators.
+cudaError_t launch_chem_call_adjoint(int ns, const hf_patch& P, const double* U, const double* ubar_out,
+                                     double* ubar_in, double dt, double rtol, double atol, double* tape, int cap,
+                                     int64_t i0, int64_t chunk, double* pcell, DevStatus* st, cudaStream_t s,
+                                     int64_t* launches);
+// Adjoint of one Euler stage (hf_flux_adjoint.cu): U is the ghost-filled stage input,
+// outbar the cotangent of the stage output, ch the stage's weight in the output (1, or
+// 1/2 with a Heun combination), h the stage length; inbar receives the interior
+// cotangent of U.  FAx / FAy: 4 NV (nx+1) ny and 4 NV nx (ny+1) doubles; UG: a
+// ghosted array of the patch's layout.
+cudaError_t launch_stage_adjoint(int ns, const Level& L, const hf_patch& P, const double* U, const double* outbar,
+                                 double ch, double h, int first_order, double* FAx, double* FAy, double* UG,
+                                 double* inbar, DevStatus* st, cudaStream_t s, int64_t* launches);
 size_t adjoint_bytes_per_cell(int ns, int ncalls, int K, int cap);
 cudaError_t launch_chem_adjoint(int ns, const AdjointArgs& a, cudaStream_t s, int64_t* launches);
 cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const int64_t* cell_index,

@@ -14,6 +14,7 @@ rhoY_0..rhoY_{NS-1}, rho*u, rho*v, rho*E (src/solver.hpp:17-25).
 """
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -390,6 +391,78 @@ class ChemObjective(torch.autograd.Function):
             sens.ctx.set_rate_scale(None)
         g = (torch.nan_to_num(G, nan=0.0) * torch.nan_to_num(gJ, nan=0.0)[None, :]).sum(1)
         return g.to(ln_mult.device, ln_mult.dtype), None, None
+
+
+class FlowAdjoint:
+    """A recorded run of Strang steps on a one-patch level and its discrete adjoint
+    (hf_flow_record / hf_flow_adjoint; an extension, the reference has no sensitivity
+    code).  The run uses the plain forms with the given step sizes (or CFL steps,
+    recorded); `final` is its final state and `dts` its step sizes.
+
+        fa = FlowAdjoint(ctx, level, U0, nsteps=1000, checkpoint_every=50)
+        U0_bar, dJ_dlnA = fa.adjoint(seed)   # seed = dJ/dU_final, (NV, ny, nx) CUDA
+    """
+
+    def __init__(self, ctx, level, U0, nsteps, dts=None, cfl=0.5, checkpoint_every=50, chemistry=True, rtol=1e-8,
+                 atol=1e-15):
+        _need_cuda64(U0, "U0")
+        self.ctx = ctx
+        U0 = U0.contiguous()
+        self.shape = tuple(U0.shape)
+        self.final = torch.empty_like(U0)
+        self.dts = np.zeros(int(nsteps))
+        d = None if dts is None else np.ascontiguousarray(dts, dtype=np.float64)
+        h = ctypes.c_void_p()
+        torch.cuda.synchronize()
+        st = ctx.lib.hf_flow_record(ctx.h, ctypes.byref(level), _ptr(U0), int(nsteps),
+                                    None if d is None else d.ctypes.data, float(cfl), int(checkpoint_every),
+                                    int(bool(chemistry)), float(rtol), float(atol), _ptr(self.final),
+                                    self.dts.ctypes.data, ctypes.byref(h), _stream())
+        ctx.check(st, "flow_record")
+        self.h = h
+
+    def adjoint(self, seed):
+        """seed: dJ/dU_final, (NV, ny, nx) float64 CUDA -> (dJ/dU0 tensor, dJ/d ln A (21,) numpy)."""
+        _need_cuda64(seed, "seed")
+        seed = seed.contiguous()
+        U0b = torch.empty(self.shape, dtype=torch.float64, device=seed.device)
+        g = np.zeros(21)
+        self.ctx.check(self.ctx.lib.hf_flow_adjoint(self.h, _ptr(seed), _ptr(U0b), g.ctypes.data, _stream()),
+                       "flow_adjoint")
+        return U0b, g
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.hf_flow_tape_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def induction_length(U, dx, product=2, sharp=4):
+    """Induction length of a right-running planar detonation from a state (NV, ny, nx)
+    (torch or numpy, differentiable in torch): the distance between the shock and the
+    reaction front, each located as the centroid of a sharpened jump,
+        x_s = sum x_f w_f / sum w_f,  w_f = (rho_i - rho_{i+1})^sharp   (density drop
+              at the leading shock),
+        x_r = sum x_f v_f / sum v_f,  v_f = (Y_i - Y_{i+1})^sharp with Y the product
+              (H2O, species index `product`) mass fraction,
+    over the faces x_f = (i + 1) dx between cells i and i+1, rows averaged.  A
+    build-defined objective: the reference defines no induction length."""
+    xp = torch if isinstance(U, torch.Tensor) else np
+    ns = U.shape[0] - 3
+    rho = U[:ns].sum(0).mean(0)
+    Y = (U[product] / U[:ns].sum(0)).mean(0)
+    nx = rho.shape[0]
+    xf = (xp.arange(1, nx, dtype=rho.dtype) if xp is np else torch.arange(1, nx, dtype=rho.dtype, device=rho.device))
+    xf = xf * dx
+    w = (rho[:-1] - rho[1:]) ** sharp
+    v = (Y[:-1] - Y[1:]) ** sharp
+    return (xf * w).sum() / w.sum() - (xf * v).sum() / v.sum()
 
 
 # ------------------------------------------------------------------ stepper

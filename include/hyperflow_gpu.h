@@ -232,6 +232,31 @@ HF_EXPORT hf_status hf_chem_adjoint(hf_ctx* ctx, const double* U0, int64_t comp_
                                     int32_t ncalls, const hf_adjoint_opts* opts, double* objective, double* dJ_dlnA,
                                     double* dJ_dY0, int64_t* first_failed, void* stream);
 
+/* ---- Discrete adjoint of a run of Strang steps (build-defined extension) ----
+ * hf_flow_record replays nsteps steps of BlockAMR::run (BlockAMR.cpp:409-419) on a one-patch
+ * level from U0 (SoA [NV][ny][nx], device) with the plain forms (ghost fill + face/update
+ * kernels, one thread per cell chemistry), each stage redone first order when its output is
+ * inadmissible (:257-263).  dts (host, nsteps) gives the step sizes; NULL: the CFL dt of
+ * each step with cfl.  It records the step sizes (dts_out, host, may be NULL), the stages'
+ * first-order flags and the state every checkpoint_every steps, and writes the final state
+ * to U_final (device SoA, may be NULL).  No wedge boundary.  Errors as the ABI calls it
+ * makes (a stage inadmissible even first order: HF_ERR_INADMISSIBLE; no dt halving). */
+typedef struct hf_flow_tape hf_flow_tape;
+HF_EXPORT hf_status hf_flow_record(hf_ctx* ctx, const hf_level* level, const double* U0, int32_t nsteps,
+                                   const double* dts, double cfl, int32_t checkpoint_every, int chemistry,
+                                   double rtol, double atol, double* U_final, double* dts_out, hf_flow_tape** out,
+                                   void* stream);
+/* Reverse sweep of a recorded run from seed = dJ/dU_final (device SoA): U0_bar = dJ/dU0
+ * (device SoA, may be NULL) and dJ_dlnA[21] (host, may be NULL) = dJ/d ln A_r (rate
+ * multipliers as hf_chem_adjoint).  The derivative of the frozen map: the recorded step
+ * sizes and every branch of the forward (minmod selections, first-order fallbacks, HLLC wave
+ * cases, wall overrides, chemistry step sequences and clips) are held fixed; roundoff
+ * repairs count as the identity.  Segments of checkpoint_every steps are recomputed from
+ * their checkpoint. */
+HF_EXPORT hf_status hf_flow_adjoint(hf_flow_tape* tape, const double* seed, double* U0_bar, double* dJ_dlnA,
+                                    void* stream);
+HF_EXPORT void hf_flow_tape_destroy(hf_flow_tape* tape);
+
 /* Chemistry without any device allocation.  No counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc: code running while a stream is being captured

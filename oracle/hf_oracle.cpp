@@ -212,8 +212,11 @@ double troe_F(const Reaction& rx, double T, double Pr, double* dlnF_dlnPr = null
 // forward rate constant, and with it the reverse one, is scaled by multiplier_r;
 // for falloff reactions both limits are scaled, so Pr is unchanged.  Per thread,
 // so finite-difference runs of different cells can perturb different reactions.
+// A process-wide set (or_set_rate_mult) applies where no per-thread set is active.
 thread_local const double* tl_rate_mult = nullptr;
-inline double rate_mult(int r) { return tl_rate_mult ? tl_rate_mult[r] : 1.0; }
+double g_rate_mult[NR];
+bool g_rate_mult_on = false;
+inline double rate_mult(int r) { return tl_rate_mult ? tl_rate_mult[r] : (g_rate_mult_on ? g_rate_mult[r] : 1.0); }
 
 // Rates of progress (kmol/m^3/s) at T and molar concentrations C.
 void progress(double T, const double* C, Rates& out) {
@@ -773,6 +776,12 @@ struct or_grid {
     double inlet[MAXV];    // the fixed inflow state ("fresh", BlockAMR.cpp:67,132-136)
     double wedge_start;
 };
+
+// Rate multipliers for every later call (null: none).
+void or_set_rate_mult(const double* m) {
+    g_rate_mult_on = m != nullptr;
+    if (m) for (int r = 0; r < NR; ++r) g_rate_mult[r] = m[r];
+}
 
 int or_set_species(int ns) {
     if (ns != 9 && ns != 10) return -1;

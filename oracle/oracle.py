@@ -66,6 +66,7 @@ def lib():
         L.or_chem_batch.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int, _lp]
         L.or_rodas4_circle.argtypes = [_dp, ctypes.c_double, ctypes.c_int]
+        L.or_set_rate_mult.argtypes = [_dp]
         L.or_chem_objective.restype = ctypes.c_int64
         L.or_chem_objective.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_int, _dp]
@@ -201,6 +202,15 @@ def chem_batch(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
 
 
 OBJECTIVES = {"ignition_delay": 0, "peak_pressure": 1, "final_T": 2}
+
+
+def set_rate_mult(mult=None):
+    """Rate multipliers (NR) for every later oracle call; None resets them."""
+    if mult is None:
+        lib().or_set_rate_mult(None)
+    else:
+        m = np.ascontiguousarray(mult, dtype=np.float64)
+        lib().or_set_rate_mult(_p(m))
 
 
 def chem_objective(U, dt, nsub, objective, dT=400.0, rtol=1e-8, atol=1e-15, mult=None, threads=0):
