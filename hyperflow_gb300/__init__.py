@@ -4,11 +4,11 @@ The compute path is libhyperflow_gpu.so (hand-written CUDA for sm_103a behind th
 C ABI of include/hyperflow_gpu.h); this package binds it with ctypes and keeps the
 reference's per-block names (see solver.py).  There is no CPU fallback.
 """
-from .solver import (ChemistryBatch, ChemObjective, ChemSensitivity, ConservativeInterp, Context,  # noqa
+from .solver import (AmrStepper, ChemistryBatch, ChemObjective, ChemSensitivity, ConservativeInterp, Context,  # noqa
                      DomainError, FlowAdjoint, HyperFlowError, PatchArray, PatchSet, Stepper, admissible,
                      average_down, cfl_dt, euler_stage, fill, hllc, induction_length, make_level, properties, reflux,
                      tag_cells, totals, validate)
 
-__all__ = ["ChemistryBatch", "ChemObjective", "ChemSensitivity", "ConservativeInterp", "Context", "DomainError",
+__all__ = ["AmrStepper", "ChemistryBatch", "ChemObjective", "ChemSensitivity", "ConservativeInterp", "Context", "DomainError",
            "FlowAdjoint", "HyperFlowError", "induction_length", "PatchArray", "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage",
            "fill", "hllc", "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]

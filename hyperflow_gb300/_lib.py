@@ -58,6 +58,11 @@ class TagCriteria(ctypes.Structure):
                 ("velocity", _d * 2)]
 
 
+class AmrOpts(ctypes.Structure):
+    _fields_ = [("max_level", _i32), ("block", _i32), ("tag_buffer", _i32), ("regrid_interval", _i32),
+                ("chemistry", _i32), ("chem_form", _i32), ("rtol", _d), ("atol", _d), ("tags", TagCriteria)]
+
+
 # (name, restype, argtypes) for every entry point of the header
 SIGNATURES = [
     ("hf_init", _i32, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -78,6 +83,15 @@ SIGNATURES = [
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
     ("hf_fp64_peak", _i32, [_vp, _dp, _vp]),
+    ("hf_amr_create", _i32, [_vp, ctypes.POINTER(Level), _vp, ctypes.POINTER(AmrOpts), ctypes.POINTER(_vp), _vp]),
+    ("hf_amr_destroy", None, [_vp]),
+    ("hf_amr_step", _i32, [_vp, _d, _dp, _vp]),
+    ("hf_amr_regrid", _i32, [_vp, _vp]),
+    ("hf_amr_info", _i32, [_vp, ctypes.c_int, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                           ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i64)]),
+    ("hf_amr_get_level", _i32, [_vp, ctypes.c_int, _vp, _vp, _vp]),
+    ("hf_amr_totals", _i32, [_vp, _dp, _vp]),
+    ("hf_amr_time", _d, [_vp]),
     ("hf_flow_record", _i32, [_vp, ctypes.POINTER(Level), _vp, _i32, _vp, _d, _i32, ctypes.c_int, _d, _d, _vp, _vp,
                               ctypes.POINTER(_vp), _vp]),
     ("hf_flow_adjoint", _i32, [_vp, _vp, _vp, _vp, _vp]),

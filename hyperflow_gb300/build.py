@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhyperflow_gpu.so")
 SOURCES = ["hf_flux.cu", "hf_chem.cu", "hf_amr.cu", "hf_abi.cu", "hf_stepper.cu", "hf_adjoint.cu",
-           "hf_flux_adjoint.cu", "hf_flow_adjoint.cu"]
+           "hf_flux_adjoint.cu", "hf_flow_adjoint.cu", "hf_amr_stepper.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "--expt-relaxed-constexpr", "-lineinfo", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]

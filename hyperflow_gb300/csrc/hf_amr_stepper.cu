@@ -1,0 +1,534 @@
+// Multi-level block-AMR time stepper over the C ABI: the loop of BlockAMR::run
+// (HyperFlow_V3/src/BlockAMR.cpp:400-439) on levels 0..max_level at refinement ratio 2
+// with no time subcycling (every level advances with the same dt, the reference's
+// summary field time_subcycling:false).
+//
+// Layout: each level is one dense ghosted SoA array over its whole domain (the base
+// domain times 2^l), 2 ghost layers; its active blocks (block x block cells, aligned)
+// are hf_patch views into that array, so same-level neighbours are read in place.
+// Memory is what a GB300 has plenty of; the dense arrays keep every index computation
+// affine and make regridding a change of the block list.
+//
+// Per stage (BlockAMR::euler, :202-264): ghosts of every level are filled (physical
+// boundaries and in-place neighbours by hf_fill_ghosts, coarse-fine ghosts by
+// ConservativeInterp from the next coarser level, coarse levels first), every level's
+// active blocks take the Euler update with face fluxes kept, then finest to coarsest:
+// reflux of the coarse level from the fine fluxes (FluxRegister) and average_down.
+// A stage inadmissible at second order is redone first order on all levels.
+// flow(h) = two stages and the Heun combination (:266-270); react(dt) advances the
+// leaf cells of every level (:271-285); a failed step rolls back and halves dt.
+//
+// Regrid (:367-373, AMReX regrid with ErrorEst tags :170-200): for l = 0..max_level-1,
+// ErrorEst on level l (ghosts filled); a block of level l+1 is active when a tagged
+// level-l cell lies in its footprint grown by tag_buffer cells and its footprint grown
+// by 2 coarse cells lies in active level-l blocks (proper nesting for the coarse-fine
+// ghost interpolation); both footprints wrap across periodic edges.  Blocks that
+// become active are filled by ConservativeInterp from level l; blocks that stay keep
+// their data.  The block choice is a deterministic function of the tags (the
+// reference's Berger-Rigoutsos clustering lives in AMReX).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "hf_internal.h"
+#include "mech_h2li.h"
+
+namespace {
+
+struct AmrLevel {
+    hf_level L{};
+    hf_patch dom{};                 // the whole level domain as one patch view
+    int nbx = 0, nby = 0;
+    std::vector<uint8_t> active;    // [nby][nbx]
+    std::vector<hf_patch> patches;  // active blocks, row-major block order
+    size_t bytes = 0;
+    double *U = nullptr, *S = nullptr, *N = nullptr, *O = nullptr, *B = nullptr;  // state, stage, next, old, backup
+    double *fx = nullptr, *fy = nullptr;  // face fluxes packed per patch (capacity: every block)
+    int64_t* cells = nullptr;             // leaf cells (device gather list)
+    int64_t nleaf = 0;
+    uint8_t* leaf_mask = nullptr;         // per patch cells, 1 = leaf (device)
+    hf_chem_history hist{nullptr, nullptr};
+};
+
+__global__ void k_lincomb_all(int64_t n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = a * x[i] + b * y[i];
+}
+
+}  // namespace
+
+struct hf_amr {
+    hf_ctx* ctx = nullptr;
+    hf_amr_opts o{};
+    int ns = 9, nv = 12;
+    std::vector<AmrLevel> lev;  // 0..max_level, allocated up front
+    int finest = 0;
+    double time = 0.0;
+    int64_t steps = 0, regrids = 0;
+};
+
+namespace {
+
+hf_status cuda_st(cudaError_t e) { return e == cudaSuccess ? HF_OK : HF_ERR_CUDA; }
+
+hf_patch block_patch(const AmrLevel& a, int bi, int bj, int B) {
+    hf_patch p = a.dom;
+    p.ilo = bi * B;
+    p.jlo = bj * B;
+    p.nx = std::min(B, a.L.nx - p.ilo);
+    p.ny = std::min(B, a.L.ny - p.jlo);
+    p.offset = (int64_t)p.jlo * a.dom.pitch + p.ilo;
+    return p;
+}
+
+// Rebuilds patches, leaf lists and leaf masks of every level from the active maps.
+hf_status rebuild(hf_amr* m, cudaStream_t s) {
+    const int B = m->o.block;
+    for (int l = 0; l <= m->o.max_level; ++l) {
+        AmrLevel& a = m->lev[l];
+        a.patches.clear();
+        if (l <= m->finest)
+            for (int bj = 0; bj < a.nby; ++bj)
+                for (int bi = 0; bi < a.nbx; ++bi)
+                    if (a.active[(size_t)bj * a.nbx + bi]) a.patches.push_back(block_patch(a, bi, bj, B));
+    }
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        const AmrLevel* f = l < m->finest ? &m->lev[l + 1] : nullptr;
+        std::vector<int64_t> idx;
+        std::vector<uint8_t> mask;
+        for (const hf_patch& p : a.patches)
+            for (int j = 0; j < p.ny; ++j)
+                for (int i = 0; i < p.nx; ++i) {
+                    const int gi = p.ilo + i, gj = p.jlo + j;
+                    // covered when the fine block over (2gi, 2gj) is active
+                    const bool covered = f && f->active[(size_t)((2 * gj) / B) * f->nbx + (2 * gi) / B];
+                    mask.push_back(covered ? 0 : 1);
+                    if (!covered) idx.push_back((int64_t)(gj + a.dom.ng) * a.dom.pitch + (gi + a.dom.ng));
+                }
+        a.nleaf = (int64_t)idx.size();
+        if (cudaMemcpyAsync(a.cells, idx.data(), sizeof(int64_t) * idx.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(a.leaf_mask, mask.data(), mask.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemsetAsync(a.hist.h, 0, sizeof(double) * std::max<int64_t>(a.nleaf, 1), s) != cudaSuccess ||
+            cudaMemsetAsync(a.hist.cost, 0, sizeof(int32_t) * std::max<int64_t>(a.nleaf, 1), s) != cudaSuccess)
+            return HF_ERR_CUDA;
+    }
+    return cuda_st(cudaStreamSynchronize(s));
+}
+
+// Block index nb along a direction with nblk blocks: wrapped when the direction is
+// periodic, -1 when it lies outside a non-periodic domain.
+int wrap_block(int nb, int nblk, int periodic) {
+    if (nb >= 0 && nb < nblk) return nb;
+    return periodic ? (nb + nblk) % nblk : -1;
+}
+
+// Cell index g along a direction with n cells: wrapped when periodic, -1 outside.
+int wrap_cell(int g, int n, int periodic) {
+    if (g >= 0 && g < n) return g;
+    return periodic ? ((g % n) + n) % n : -1;
+}
+
+// Coarse-fine ghosts of level l's blocks: the 2-cell frame parts that lie in inactive
+// blocks (across a periodic boundary: the inactive periodic image), by
+// ConservativeInterp from level l-1.  A frame part outside a non-periodic domain
+// edge holds physical ghosts.  Across a periodic edge the region is interpolated in
+// place from the coarse level's ghost frame, which holds the periodic image.
+hf_status fill_cf(hf_amr* m, int l, double* Uf, const double* Uc, cudaStream_t s) {
+    const AmrLevel& a = m->lev[l];
+    const AmrLevel& c = m->lev[l - 1];
+    const int B = m->o.block;
+    for (const hf_patch& p : a.patches) {
+        const int bi = p.ilo / B, bj = p.jlo / B;
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di) {
+                if (!di && !dj) continue;
+                const int nbi = wrap_block(bi + di, a.nbx, a.L.periodic[0]);
+                const int nbj = wrap_block(bj + dj, a.nby, a.L.periodic[1]);
+                if (nbi < 0 || nbj < 0) continue;                   // outside: physical ghosts
+                if (a.active[(size_t)nbj * a.nbx + nbi]) continue;  // in place (or periodic copy)
+                int32_t r[4];
+                r[0] = di < 0 ? p.ilo - 2 : (di > 0 ? p.ilo + p.nx : p.ilo);
+                r[2] = di < 0 ? p.ilo - 1 : (di > 0 ? p.ilo + p.nx + 1 : p.ilo + p.nx - 1);
+                r[1] = dj < 0 ? p.jlo - 2 : (dj > 0 ? p.jlo + p.ny : p.jlo);
+                r[3] = dj < 0 ? p.jlo - 1 : (dj > 0 ? p.jlo + p.ny + 1 : p.jlo + p.ny - 1);
+                hf_status q = hf_interp_coarse_to_fine(m->ctx, &c.dom, Uc, &p, Uf, r, s);
+                if (q != HF_OK) return q;
+            }
+    }
+    return HF_OK;
+}
+
+// Ghosts of every level of the arrays X[l] (coarse levels first).
+hf_status fill_all(hf_amr* m, double* const* X, cudaStream_t s) {
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        hf_status r = hf_fill_ghosts(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), X[l], s);
+        if (r == HF_OK && l > 0) r = fill_cf(m, l, X[l], X[l - 1], s);
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
+}
+
+// One composite Euler stage in -> out (BlockAMR::euler).
+hf_status euler(hf_amr* m, double* const* in, double* const* out, double h, cudaStream_t s) {
+    hf_status r = fill_all(m, in, s);
+    if (r != HF_OK) return r;
+    for (int fo = 0; fo < 2; ++fo) {
+        r = HF_OK;
+        for (int l = 0; r == HF_OK && l <= m->finest; ++l) {
+            AmrLevel& a = m->lev[l];
+            int64_t bad = -1;
+            r = hf_flux_update(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), in[l], nullptr, out[l], a.fx, a.fy,
+                               h, fo, HF_FLUX_PLAIN, &bad, s);
+        }
+        if (r == HF_OK) {
+            if (fo) hf::ctx_add_counters(m->ctx, 1, 0);
+            break;
+        }
+        if (r != HF_ERR_INADMISSIBLE && r != HF_ERR_NEGATIVE) return r;
+    }
+    if (r != HF_OK) return r;
+    for (int l = m->finest; l > 0; --l) {
+        AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
+        r = hf_reflux(m->ctx, &c.L, c.patches.data(), (int)c.patches.size(), out[l - 1], c.fx, c.fy, f.patches.data(),
+                      (int)f.patches.size(), f.fx, f.fy, h, s);
+        if (r == HF_OK)
+            r = hf_average_down(m->ctx, f.patches.data(), (int)f.patches.size(), out[l], c.patches.data(),
+                                (int)c.patches.size(), out[l - 1], s);
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
+}
+
+hf_status average_all(hf_amr* m, double* const* X, cudaStream_t s) {
+    for (int l = m->finest; l > 0; --l) {
+        AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
+        hf_status r = hf_average_down(m->ctx, f.patches.data(), (int)f.patches.size(), X[l], c.patches.data(),
+                                      (int)c.patches.size(), X[l - 1], s);
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
+}
+
+hf_status validate_all(hf_amr* m, double* const* X, cudaStream_t s) {
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        int64_t bad = -1;
+        hf_status r = hf_validate(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), X[l], &bad, s);
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
+}
+
+template <class F>
+void arrays(hf_amr* m, F pick, double** X) {
+    for (int l = 0; l <= m->o.max_level; ++l) X[l] = pick(m->lev[l]);
+}
+
+// flow(h): U <- (U + E(E(U)))/2 on every level (BlockAMR::flow, :266-270).
+hf_status flow(hf_amr* m, double h, cudaStream_t s) {
+    double *U[8], *S[8], *N[8];
+    arrays(m, [](AmrLevel& a) { return a.U; }, U);
+    arrays(m, [](AmrLevel& a) { return a.S; }, S);
+    arrays(m, [](AmrLevel& a) { return a.N; }, N);
+    hf_status r = euler(m, U, S, h, s);
+    if (r == HF_OK) r = euler(m, S, N, h, s);
+    if (r != HF_OK) return r;
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        const int64_t n = (int64_t)(a.bytes / sizeof(double));
+        k_lincomb_all<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 0.5, a.U, 0.5, a.N);
+        if (cudaGetLastError() != cudaSuccess) return HF_ERR_CUDA;
+    }
+    r = average_all(m, N, s);
+    if (r == HF_OK) r = validate_all(m, N, s);
+    if (r != HF_OK) return HF_ERR_COMBINE;
+    for (int l = 0; l <= m->finest; ++l) std::swap(m->lev[l].U, m->lev[l].N);
+    return HF_OK;
+}
+
+// react(dt) on the leaf cells of every level (BlockAMR::react, :271-285).
+hf_status react(hf_amr* m, double dt, cudaStream_t s) {
+    if (!m->o.chemistry) return HF_OK;
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        if (!a.nleaf) continue;
+        int64_t first = -1;
+        hf_status r = m->o.chem_form == HF_CHEM_PERSISTENT
+                          ? hf_chem_advance_batched(m->ctx, a.U, a.dom.comp_stride, a.cells, a.nleaf, dt, nullptr,
+                                                    m->o.rtol, m->o.atol, &a.hist, &first, s)
+                          : hf_chem_advance(m->ctx, a.U, a.dom.comp_stride, a.cells, a.nleaf, dt, nullptr, m->o.rtol,
+                                            m->o.atol, m->o.chem_form, &first, s);
+        if (r != HF_OK) return r;
+    }
+    double* U[8];
+    arrays(m, [](AmrLevel& a) { return a.U; }, U);
+    hf_status r = average_all(m, U, s);
+    if (r == HF_OK) r = validate_all(m, U, s);
+    return r;
+}
+
+hf_status totals(hf_amr* m, double* out, cudaStream_t s, int absolute = 0) {
+    for (int n = 0; n < m->nv; ++n) out[n] = 0.0;
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        double t[16];
+        hf_status r = hf_totals(m->ctx, a.patches.data(), (int)a.patches.size(), a.U, a.leaf_mask, a.L.dx * a.L.dy,
+                                absolute, t, s);
+        if (r != HF_OK) return r;
+        for (int n = 0; n < m->nv; ++n) out[n] += t[n];
+    }
+    return HF_OK;
+}
+
+// New active blocks of level l+1 from the tags of level l.
+hf_status regrid_level(hf_amr* m, int l, cudaStream_t s) {
+    AmrLevel& c = m->lev[l];
+    AmrLevel& f = m->lev[l + 1];
+    const int B = m->o.block, half = B / 2, buf = m->o.tag_buffer;
+    double* U[8];
+    arrays(m, [](AmrLevel& a) { return a.U; }, U);
+    hf_status r = fill_all(m, U, s);  // ErrorEst reads the neighbours
+    if (r != HF_OK) return r;
+    int64_t ncell = 0;
+    for (const hf_patch& p : c.patches) ncell += (int64_t)p.nx * p.ny;
+    uint8_t* dtags = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&dtags), std::max<int64_t>(ncell, 1), s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    r = hf_tag_cells(m->ctx, &c.L, c.patches.data(), (int)c.patches.size(), c.U, m->time, &m->o.tags, dtags, s);
+    std::vector<uint8_t> tags(ncell);
+    if (r == HF_OK)
+        r = cuda_st(cudaMemcpyAsync(tags.data(), dtags, ncell, cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(dtags, s);
+    if (r == HF_OK) r = cuda_st(cudaStreamSynchronize(s));
+    if (r != HF_OK) return r;
+    // tagged and active maps of level l (cell resolution)
+    std::vector<uint8_t> tag((size_t)c.L.nx * c.L.ny, 0), act((size_t)c.L.nx * c.L.ny, 0);
+    int64_t k = 0;
+    for (const hf_patch& p : c.patches)
+        for (int j = 0; j < p.ny; ++j)
+            for (int i = 0; i < p.nx; ++i, ++k) {
+                const size_t g = (size_t)(p.jlo + j) * c.L.nx + (p.ilo + i);
+                tag[g] = tags[k];
+                act[g] = 1;
+            }
+    std::vector<uint8_t> next(f.active.size(), 0);
+    for (int bj = 0; bj < f.nby; ++bj)
+        for (int bi = 0; bi < f.nbx; ++bi) {
+            // footprint of the fine block on level l
+            const int i0 = bi * half, j0 = bj * half;
+            const int i1 = std::min(i0 + half, c.L.nx) - 1, j1 = std::min(j0 + half, c.L.ny) - 1;
+            // both footprints wrap across periodic edges and are cut at the others
+            const int px = c.L.periodic[0], py = c.L.periodic[1];
+            bool tagged = false;
+            for (int jj = j0 - buf; !tagged && jj <= j1 + buf; ++jj)
+                for (int ii = i0 - buf; ii <= i1 + buf; ++ii) {
+                    const int i = wrap_cell(ii, c.L.nx, px), j = wrap_cell(jj, c.L.ny, py);
+                    if (i >= 0 && j >= 0 && tag[(size_t)j * c.L.nx + i]) { tagged = true; break; }
+                }
+            if (!tagged) continue;
+            bool nested = true;
+            for (int jj = j0 - 2; nested && jj <= j1 + 2; ++jj)
+                for (int ii = i0 - 2; ii <= i1 + 2; ++ii) {
+                    const int i = wrap_cell(ii, c.L.nx, px), j = wrap_cell(jj, c.L.ny, py);
+                    if (i >= 0 && j >= 0 && !act[(size_t)j * c.L.nx + i]) { nested = false; break; }
+                }
+            next[(size_t)bj * f.nbx + bi] = nested ? 1 : 0;
+        }
+    // blocks that become active: ConservativeInterp from level l
+    std::vector<uint8_t> prev = f.active;
+    const bool had = m->finest >= l + 1;
+    f.active = next;
+    int any = 0;
+    for (uint8_t v : next) any |= v;
+    m->finest = any ? std::max(m->finest, l + 1) : l;
+    for (int bj = 0; bj < f.nby; ++bj)
+        for (int bi = 0; bi < f.nbx; ++bi) {
+            const size_t b = (size_t)bj * f.nbx + bi;
+            if (!next[b] || (had && prev[b])) continue;
+            const hf_patch p = block_patch(f, bi, bj, B);
+            const int32_t reg[4] = {p.ilo, p.jlo, p.ilo + p.nx - 1, p.jlo + p.ny - 1};
+            r = hf_interp_coarse_to_fine(m->ctx, &c.dom, c.U, &p, f.U, reg, s);
+            if (r != HF_OK) return r;
+        }
+    if (!any)
+        for (int q = l + 2; q <= m->o.max_level; ++q) std::fill(m->lev[q].active.begin(), m->lev[q].active.end(), 0);
+    return rebuild(m, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+hf_status hf_amr_regrid(hf_amr* m, void* stream) {
+    if (!m) return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    double before[16], after[16], scale[16];
+    hf_status r = totals(m, before, s);
+    if (r == HF_OK) r = totals(m, scale, s, 1);
+    for (int l = 0; r == HF_OK && l < m->o.max_level && l <= m->finest; ++l) r = regrid_level(m, l, s);
+    if (r == HF_OK) r = totals(m, after, s);
+    if (r != HF_OK) return r;
+    ++m->regrids;
+    // regridChecked (:369-371): the conserved totals must survive the remap (relative to
+    // the total of the magnitudes, so that a component summing to ~0 is judged fairly)
+    for (int n = 0; n < m->nv; ++n)
+        if (std::fabs(after[n] - before[n]) > 1e-8 * scale[n]) return HF_ERR_INADMISSIBLE;
+    return HF_OK;
+}
+
+hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, const hf_amr_opts* o, hf_amr** out,
+                        void* stream) {
+    if (out) *out = nullptr;
+    if (!ctx || !base || !U0 || !o || !out || o->max_level < 0 || o->max_level > 6 || o->block < 8 ||
+        (o->block & 1) || base->nx % (o->block / 2) || base->ny % (o->block / 2) || o->tag_buffer < 0 ||
+        !(o->rtol > 0) || !(o->atol > 0))
+        return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    hf_amr* m = new hf_amr();
+    m->ctx = ctx;
+    m->o = *o;
+    m->ns = hf_nspecies(ctx);
+    m->nv = m->ns + 3;
+    m->lev.resize(o->max_level + 1);
+    bool ok = true;
+    for (int l = 0; ok && l <= o->max_level; ++l) {
+        AmrLevel& a = m->lev[l];
+        a.L = *base;
+        a.L.nx = base->nx << l;
+        a.L.ny = base->ny << l;
+        a.L.dx = base->dx / (1 << l);
+        a.L.dy = base->dy / (1 << l);
+        hf_patch& d = a.dom;
+        d.ilo = d.jlo = 0;
+        d.nx = a.L.nx;
+        d.ny = a.L.ny;
+        d.ng = 2;
+        d.pitch = (d.nx + 2 * d.ng + 1) & ~int64_t(1);
+        d.comp_stride = (d.pitch * (d.ny + 2 * d.ng) + 31) & ~int64_t(31);
+        d.offset = 0;
+        a.nbx = (a.L.nx + o->block - 1) / o->block;
+        a.nby = (a.L.ny + o->block - 1) / o->block;
+        a.active.assign((size_t)a.nbx * a.nby, l == 0 ? 1 : 0);
+        a.bytes = sizeof(double) * (size_t)d.comp_stride * m->nv;
+        const int64_t nc = (int64_t)a.L.nx * a.L.ny;
+        const size_t fb = sizeof(double) * (size_t)m->nv * ((size_t)(a.L.nx + a.nbx) * a.L.ny);
+        const size_t gb = sizeof(double) * (size_t)m->nv * ((size_t)a.L.nx * (a.L.ny + a.nby));
+        for (double** p : {&a.U, &a.S, &a.N, &a.O, &a.B})
+            ok = ok && cudaMalloc(p, a.bytes) == cudaSuccess && cudaMemset(*p, 0, a.bytes) == cudaSuccess;
+        ok = ok && cudaMalloc(&a.fx, fb) == cudaSuccess && cudaMalloc(&a.fy, gb) == cudaSuccess &&
+             cudaMalloc(&a.cells, sizeof(int64_t) * nc) == cudaSuccess && cudaMalloc(&a.leaf_mask, nc) == cudaSuccess &&
+             cudaMalloc(&a.hist.h, sizeof(double) * nc) == cudaSuccess &&
+             cudaMalloc(&a.hist.cost, sizeof(int32_t) * nc) == cudaSuccess;
+    }
+    if (ok) {
+        AmrLevel& a = m->lev[0];
+        const int64_t nc = (int64_t)a.L.nx * a.L.ny;
+        for (int n = 0; ok && n < m->nv; ++n)
+            ok = cudaMemcpy2DAsync(a.U + n * a.dom.comp_stride + a.dom.ng * a.dom.pitch + a.dom.ng,
+                                   a.dom.pitch * sizeof(double), U0 + (size_t)n * nc, a.L.nx * sizeof(double),
+                                   a.L.nx * sizeof(double), a.L.ny, cudaMemcpyDeviceToDevice, s) == cudaSuccess;
+    }
+    hf_status r = ok ? rebuild(m, s) : HF_ERR_CUDA;
+    // initial hierarchy: one regrid per level
+    for (int k = 0; r == HF_OK && k < o->max_level; ++k) r = hf_amr_regrid(m, stream);
+    m->regrids = 0;
+    if (r != HF_OK) {
+        hf_amr_destroy(m);
+        return r;
+    }
+    *out = m;
+    return HF_OK;
+}
+
+void hf_amr_destroy(hf_amr* m) {
+    if (!m) return;
+    for (AmrLevel& a : m->lev) {
+        for (double* p : {a.U, a.S, a.N, a.O, a.B, a.fx, a.fy}) cudaFree(p);
+        cudaFree(a.cells);
+        cudaFree(a.leaf_mask);
+        cudaFree(a.hist.h);
+        cudaFree(a.hist.cost);
+    }
+    delete m;
+}
+
+hf_status hf_amr_step(hf_amr* m, double cfl, double* dt, void* stream) {
+    if (!m || !dt) return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    double h = *dt;
+    if (!(h > 0)) {
+        // stableDt over the leaf cells of every level (:335-346): the finest level's
+        // cells bind (the coarse cells under them are their averages)
+        h = INFINITY;
+        for (int l = 0; l <= m->finest; ++l) {
+            AmrLevel& a = m->lev[l];
+            double d = 0.0;
+            hf_status r = hf_cfl_dt(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), a.U, cfl, &d, s);
+            if (r != HF_OK) return r;
+            h = std::min(h, d);
+        }
+    }
+    for (int l = 0; l <= m->finest; ++l)
+        if (cudaMemcpyAsync(m->lev[l].B, m->lev[l].U, m->lev[l].bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return HF_ERR_CUDA;
+    for (int attempt = 0; attempt < 18; ++attempt) {
+        hf_status r = flow(m, 0.5 * h, s);
+        if (r == HF_OK) r = react(m, h, s);
+        if (r == HF_OK) r = flow(m, 0.5 * h, s);
+        if (r == HF_OK) {
+            m->time += h;
+            *dt = h;
+            ++m->steps;
+            if (m->o.regrid_interval > 0 && m->steps % m->o.regrid_interval == 0) return hf_amr_regrid(m, stream);
+            return HF_OK;
+        }
+        if (r == HF_ERR_ARG || r == HF_ERR_CUDA || r == HF_ERR_TIMEOUT) return r;
+        hf::ctx_add_counters(m->ctx, 0, 1);
+        for (int l = 0; l <= m->finest; ++l)
+            if (cudaMemcpyAsync(m->lev[l].U, m->lev[l].B, m->lev[l].bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return HF_ERR_CUDA;
+        h *= 0.5;  // rollback (:413-418)
+    }
+    return HF_ERR_INADMISSIBLE;
+}
+
+hf_status hf_amr_info(const hf_amr* m, int lev, int32_t* nx, int32_t* ny, int32_t* nbx, int32_t* nby,
+                      int32_t* finest, int64_t* leaf_cells) {
+    if (!m || lev < 0 || lev > m->o.max_level) return HF_ERR_ARG;
+    const AmrLevel& a = m->lev[lev];
+    if (nx) *nx = a.L.nx;
+    if (ny) *ny = a.L.ny;
+    if (nbx) *nbx = a.nbx;
+    if (nby) *nby = a.nby;
+    if (finest) *finest = m->finest;
+    if (leaf_cells) *leaf_cells = lev <= m->finest ? a.nleaf : 0;
+    return HF_OK;
+}
+
+hf_status hf_amr_get_level(hf_amr* m, int lev, double* U, uint8_t* active, void* stream) {
+    if (!m || lev < 0 || lev > m->o.max_level) return HF_ERR_ARG;
+    const AmrLevel& a = m->lev[lev];
+    const int64_t nc = (int64_t)a.L.nx * a.L.ny;
+    if (U)
+        for (int n = 0; n < m->nv; ++n)
+            if (cudaMemcpy2DAsync(U + (size_t)n * nc, a.L.nx * sizeof(double),
+                                  a.U + n * a.dom.comp_stride + a.dom.ng * a.dom.pitch + a.dom.ng,
+                                  a.dom.pitch * sizeof(double), a.L.nx * sizeof(double), a.L.ny,
+                                  cudaMemcpyDeviceToDevice, reinterpret_cast<cudaStream_t>(stream)) != cudaSuccess)
+                return HF_ERR_CUDA;
+    if (active)
+        for (size_t b = 0; b < a.active.size(); ++b) active[b] = lev <= m->finest ? a.active[b] : 0;
+    return HF_OK;
+}
+
+hf_status hf_amr_totals(hf_amr* m, double* out, void* stream) {
+    if (!m || !out) return HF_ERR_ARG;
+    return totals(m, out, reinterpret_cast<cudaStream_t>(stream));
+}
+
+double hf_amr_time(const hf_amr* m) { return m ? m->time : 0.0; }
+
+}  // extern "C"

@@ -311,7 +311,11 @@ cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int, co
 // with their boundary values computed from the tile (periodic images from global
 // memory), in AMReX order.  Faces are evaluated into shared memory, then each
 // thread updates, validates and (optionally) Heun-combines one cell.
-constexpr int TX = 32, TY = 8, HX = TX + 4, HY = TY + 4, NTHR = TX * TY;
+// A 32 x 7 tile has (TX+1) TY + TX (TY+1) = 487 faces, which 8 warps take in two
+// passes (a 32 x 8 tile has 552: a third, nearly empty pass that the other warps wait
+// for at the barrier); the first TX x TY threads then update one cell each.  Nine
+// warps would cap registers at 168 (three warps on one scheduler) and spill.
+constexpr int TX = 32, TY = 7, HX = TX + 4, HY = TY + 4, NTHR = 256;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -476,6 +480,7 @@ __global__ void __launch_bounds__(NTHR) k_flux_fused(const __grid_constant__ CUt
     __syncthreads();
 
     // 4. update, validate, combine
+    if (tid >= TX * TY) return;
     const int i = tid % TX, j = tid / TX;
     const int ci = ti0 + i, cj = tj0 + j;
     if (ci >= P.nx || cj >= P.ny) return;

@@ -605,9 +605,9 @@ def reflux(ctx, coarse_level, coarse, fxc, fyc, fine, fxf, fyf, h):
                                 _stream()), "reflux")
 
 
-def tag_cells(ctx, level, pset, time, pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0,
-              chemistry=True, box=None, box_only=False, velocity=(0.0, 0.0)):
-    """ErrorEst (BlockAMR.cpp:170-200) tags of the valid cells (ghost layers filled)."""
+def tag_criteria(pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0, chemistry=True,
+                 box=None, box_only=False, velocity=(0.0, 0.0)):
+    """hf_tag_criteria from the reference's case keys (BlockAMR.cpp:170-200 defaults)."""
     c = L.TagCriteria()
     c.pressure_tag, c.temperature_tag, c.fuel_rate_tag, c.density_tag = (pressure_tag, temperature_tag,
                                                                          fuel_rate_tag, density_tag)
@@ -616,7 +616,88 @@ def tag_cells(ctx, level, pset, time, pressure_tag=0.08, temperature_tag=0.08, f
         for k in range(4):
             c.box[k] = float(box[k])
     c.velocity[0], c.velocity[1] = float(velocity[0]), float(velocity[1])
+    return c
+
+
+def tag_cells(ctx, level, pset, time, pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0,
+              chemistry=True, box=None, box_only=False, velocity=(0.0, 0.0)):
+    """ErrorEst (BlockAMR.cpp:170-200) tags of the valid cells (ghost layers filled)."""
+    c = tag_criteria(pressure_tag, temperature_tag, fuel_rate_tag, density_tag, chemistry, box, box_only, velocity)
     tags = torch.zeros(pset.cells(), dtype=torch.uint8, device=pset.data.device)
     ctx.check(ctx.lib.hf_tag_cells(ctx.h, ctypes.byref(level), pset.patches, len(pset), _ptr(pset.data),
                                    float(time), ctypes.byref(c), _ptr(tags), _stream()), "tag_cells")
     return tags
+
+
+# ------------------------------------------------------------------ multi-level block AMR
+class AmrStepper:
+    """BlockAMR::run on levels 0..max_level (hf_amr_*): dense level arrays with active
+    blocks of `block` cells, no time subcycling, regrid every `regrid_interval` steps.
+
+    level: the base level (make_level); U0: (NV, ny, nx) float64 CUDA tensor; tags: keyword
+    arguments of tag_criteria (ErrorEst keys, density_tag extension)."""
+
+    def __init__(self, ctx, level, U0, max_level=1, block=32, tag_buffer=2, regrid_interval=0, chemistry=True,
+                 chem="batched", rtol=1e-8, atol=1e-15, tags=None):
+        _need_cuda64(U0, "U0")
+        self.ctx = ctx
+        o = L.AmrOpts()
+        o.max_level, o.block, o.tag_buffer, o.regrid_interval = int(max_level), int(block), int(tag_buffer), int(
+            regrid_interval)
+        o.chemistry = int(bool(chemistry))
+        o.chem_form = {"plain": L.HF_CHEM_PLAIN, "batched": L.HF_CHEM_PERSISTENT}[chem]
+        o.rtol, o.atol = float(rtol), float(atol)
+        o.tags = tag_criteria(chemistry=chemistry, **(tags or {}))
+        self.opts = o
+        self.nv = U0.shape[0]
+        h = ctypes.c_void_p()
+        torch.cuda.synchronize()
+        ctx.check(ctx.lib.hf_amr_create(ctx.h, ctypes.byref(level), _ptr(U0.contiguous()), ctypes.byref(o),
+                                        ctypes.byref(h), _stream()), "amr_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.hf_amr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt=0.0, cfl=0.5):
+        d = ctypes.c_double(float(dt))
+        self.ctx.check(self.ctx.lib.hf_amr_step(self.h, float(cfl), ctypes.byref(d), _stream()), "amr_step")
+        return d.value
+
+    def regrid(self):
+        self.ctx.check(self.ctx.lib.hf_amr_regrid(self.h, _stream()), "amr_regrid")
+
+    def info(self, lev):
+        v = [ctypes.c_int32() for _ in range(5)]
+        leaf = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.hf_amr_info(self.h, int(lev), *[ctypes.byref(x) for x in v], ctypes.byref(leaf)),
+                       "amr_info")
+        return {"nx": v[0].value, "ny": v[1].value, "nbx": v[2].value, "nby": v[3].value, "finest": v[4].value,
+                "leaf_cells": leaf.value}
+
+    def level(self, lev):
+        """(state (NV, ny_l, nx_l) CUDA tensor, block activity (nby, nbx) numpy uint8)."""
+        i = self.info(lev)
+        U = torch.empty(self.nv, i["ny"], i["nx"], dtype=torch.float64, device="cuda")
+        act = np.zeros((i["nby"], i["nbx"]), dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.hf_amr_get_level(self.h, int(lev), _ptr(U), act.ctypes.data, _stream()),
+                       "amr_get_level")
+        return U, act
+
+    def totals(self):
+        out = np.zeros(self.nv)
+        self.ctx.check(self.ctx.lib.hf_amr_totals(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                  _stream()), "amr_totals")
+        return out
+
+    @property
+    def time(self):
+        return self.ctx.lib.hf_amr_time(self.h)

@@ -106,3 +106,30 @@ def ignition_batch(n=4096, seed=0):
     X[:, M.SPECIES.index("O2")] = 1.0
     X[:, M.SPECIES.index("N2")] = 3.76
     return _cells_at_rest(T, p, X, 9)
+
+
+def wedge(nx=512, ny=256, mach=7.0, angle_deg=30.0, T0=300.0, p0=0.1 * 101325.0, length=0.032, x_tip=0.004):
+    """Oblique detonation over a wedge: stoichiometric H2/air (9 species) at p0 / T0 moving
+    at `mach` times its sound speed, rotated by angle_deg toward the bottom wall
+    (u0 = V cos a, v0 = -V sin a, the teng_osw convention of BlockAMR.cpp:61-66); the
+    bottom is the wedge surface from x = 0 on (x_tip cells of length upstream of the tip
+    keep a zero-gradient bottom), inflow at the left and top, transmissive on the right.
+    Returns (U (NV, ny, nx), level keys)."""
+    ns = 9
+    X = np.zeros(ns)
+    X[M.SPECIES.index("H2")], X[M.SPECIES.index("O2")], X[M.SPECIES.index("N2")] = 2.0, 1.0, 3.76
+    X /= X.sum()
+    W = M.MW[:ns]
+    a_lo = M.NASA_LOW[:ns]
+    cpR = float(np.sum(X * (a_lo[:, 0] + T0 * (a_lo[:, 1] + T0 * (a_lo[:, 2] + T0 * (a_lo[:, 3] + T0 * a_lo[:, 4]))))))
+    gam = cpR / (cpR - 1.0)
+    a = np.sqrt(gam * M.GAS_CONSTANT * T0 / float(np.sum(X * W)))
+    V = mach * a
+    th = np.radians(angle_deg)
+    q = M.primitive(T0, p0, X=X, u=V * np.cos(th), v=-V * np.sin(th), ns=ns)
+    dx = length / nx
+    U = np.empty((ns + 3, ny, nx))
+    U[:] = q[:, None, None]
+    level = dict(nx=nx, ny=ny, dx=dx, dy=dx, xlo=-x_tip, ylo=0.0, periodic=(0, 0),
+                 boundary_lo=("inflow", "wedge"), boundary_hi=("transmissive", "inflow"), inlet=q, wedge_start=0.0)
+    return U, level

@@ -324,6 +324,47 @@ HF_EXPORT hf_status hf_tag_cells(hf_ctx* ctx, const hf_level* level, const hf_pa
                                  const double* U, double time, const hf_tag_criteria* criteria, uint8_t* tags,
                                  void* stream);
 
+/* ---- Multi-level block AMR (BlockAMR::run with max_level > 0, BlockAMR.cpp:400-439) ----
+ * Levels 0..max_level at ratio 2 with no time subcycling; each level a dense ghosted array
+ * over its domain whose active blocks (block x block cells) are the patches.  Per stage:
+ * ghosts (physical, in-place neighbours, ConservativeInterp from the coarser level at
+ * coarse-fine boundaries), the Euler update of every level, reflux and average_down
+ * finest to coarsest, a first-order redo of the composite stage when needed; Heun
+ * combination; react() on the leaf cells; rollback and dt halving.  Regrid every
+ * regrid_interval steps (and max_level times at creation): ErrorEst tags (tags) on level l
+ * make a level-(l+1) block active when a tagged cell lies in its footprint grown by
+ * tag_buffer cells and its footprint grown by 2 cells lies in active level-l blocks; new
+ * blocks are filled by ConservativeInterp; the conserved totals are checked to 1e-8 of the
+ * totals of magnitudes (regridChecked).  base: level 0 (nx, ny multiples of block/2). */
+typedef struct hf_amr_opts {
+    int32_t max_level;        /* "max_level" */
+    int32_t block;            /* block size ("max_grid_size"), even, >= 8 */
+    int32_t tag_buffer;       /* "tag_buffer" (cells of the tagged level) */
+    int32_t regrid_interval;  /* "regrid_interval" (steps; <= 0: no regrid after creation) */
+    int32_t chemistry;        /* "chemistry" */
+    int32_t chem_form;        /* HF_CHEM_PLAIN or HF_CHEM_PERSISTENT (batched) */
+    double rtol, atol;
+    hf_tag_criteria tags;
+} hf_amr_opts;
+typedef struct hf_amr hf_amr;
+/* U0: level-0 state, SoA [NV][ny][nx] device memory (copied). */
+HF_EXPORT hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, const hf_amr_opts* opts,
+                                  hf_amr** out, void* stream);
+HF_EXPORT void hf_amr_destroy(hf_amr* amr);
+/* One Strang step of every level; *dt as hf_stepper_step (<= 0: stableDt over all levels). */
+HF_EXPORT hf_status hf_amr_step(hf_amr* amr, double cfl, double* dt, void* stream);
+HF_EXPORT hf_status hf_amr_regrid(hf_amr* amr, void* stream);
+/* Level sizes, block grid, finest level and the level's leaf cells. */
+HF_EXPORT hf_status hf_amr_info(const hf_amr* amr, int lev, int32_t* nx, int32_t* ny, int32_t* nbx, int32_t* nby,
+                                int32_t* finest, int64_t* leaf_cells);
+/* Level lev's dense state (SoA [NV][ny_l][nx_l], device; cells of inactive blocks are
+ * stale) and its block activity map ([nby][nbx], host, may be NULL). */
+HF_EXPORT hf_status hf_amr_get_level(hf_amr* amr, int lev, double* U, uint8_t* active, void* stream);
+/* Composite totals over the leaf cells of all levels (host, NV doubles). */
+HF_EXPORT hf_status hf_amr_totals(hf_amr* amr, double* out, void* stream);
+HF_EXPORT double hf_amr_time(const hf_amr* amr);
+
+
 /* ---- reductions ---- */
 /* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the valid cells of the patches:
  * *dt = cfl / max((|u|+a)/dx + (|v|+a)/dy).  HF_ERR_INADMISSIBLE if a cell is not. */

@@ -1186,6 +1186,69 @@ int or_react(const or_grid* g, double* U, double dt, double rtol, double atol, i
     return or_validate(g, U);
 }
 
+// A run of Strang steps with given step sizes whose chemistry calls record their
+// accepted step sizes (or_run_record), and its frozen replay (or_run_replay): the map
+// a discrete adjoint of the run differentiates.  No dt halving: a failed step fails.
+struct or_run_tape {
+    int nsteps = 0;
+    std::vector<double> dts;
+    std::vector<std::vector<std::vector<double>>> h;  // [step][cell] accepted step sizes
+};
+
+static int react_frozen(const or_grid* g, double* U, double dt, double rtol, double atol, int threads,
+                        std::vector<std::vector<double>>* rec, const std::vector<std::vector<double>>* rep) {
+    const int nv = NV();
+    const int64_t nc = (int64_t)g->nx * g->ny;
+    std::vector<double> batch((size_t)nc * nv);
+    for (int j = 0; j < g->ny; ++j) for (int i = 0; i < g->nx; ++i) for (int n = 0; n < nv; ++n)
+        batch[((size_t)j * g->nx + i) * nv + n] = at(g, U, i, j, n);
+    if (rec) rec->assign(nc, {});
+    std::vector<int> fail(nc, 0);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < nc; ++k) {
+        const std::vector<double>* hs = rep ? &(*rep)[k] : nullptr;
+        fail[k] = chem_substep(&batch[k * nv], dt, rtol, atol, rec ? &(*rec)[k] : nullptr, hs ? hs->data() : nullptr,
+                               hs ? (long)hs->size() : 0);
+    }
+    for (int64_t k = 0; k < nc; ++k) if (fail[k]) return 1;
+    for (int j = 0; j < g->ny; ++j) for (int i = 0; i < g->nx; ++i) for (int n = 0; n < nv; ++n)
+        at(g, U, i, j, n) = batch[((size_t)j * g->nx + i) * nv + n];
+    return or_validate(g, U);
+}
+
+void* or_run_record(const or_grid* g, double* U, int nsteps, const double* dts, double rtol, double atol,
+                    int threads) {
+    auto* t = new or_run_tape();
+    t->nsteps = nsteps;
+    t->dts.assign(dts, dts + nsteps);
+    t->h.resize(nsteps);
+    for (int n = 0; n < nsteps; ++n) {
+        const double h = dts[n];
+        if (or_flow(g, U, 0.5 * h, nullptr) || react_frozen(g, U, h, rtol, atol, threads, &t->h[n], nullptr) ||
+            or_flow(g, U, 0.5 * h, nullptr)) {
+            delete t;
+            return nullptr;
+        }
+    }
+    return t;
+}
+
+int or_run_replay(const void* tape, const or_grid* g, double* U, double rtol, double atol, int threads) {
+    const auto* t = static_cast<const or_run_tape*>(tape);
+    for (int n = 0; n < t->nsteps; ++n) {
+        const double h = t->dts[n];
+        if (or_flow(g, U, 0.5 * h, nullptr) || react_frozen(g, U, h, rtol, atol, threads, nullptr, &t->h[n]) ||
+            or_flow(g, U, 0.5 * h, nullptr))
+            return 1;
+    }
+    return 0;
+}
+
+void or_run_free(void* tape) { delete static_cast<or_run_tape*>(tape); }
+
 // BlockAMR.cpp:335-346
 double or_cfl_dt(const or_grid* g, const double* U, double cfl) {
     double rate = 0;

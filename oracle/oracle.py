@@ -67,6 +67,12 @@ def lib():
                                     ctypes.c_double, ctypes.c_int, _lp]
         L.or_rodas4_circle.argtypes = [_dp, ctypes.c_double, ctypes.c_int]
         L.or_set_rate_mult.argtypes = [_dp]
+        L.or_run_record.restype = ctypes.c_void_p
+        L.or_run_record.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int]
+        L.or_run_replay.argtypes = [ctypes.c_void_p, ctypes.POINTER(Grid), _dp, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int]
+        L.or_run_free.argtypes = [ctypes.c_void_p]
         L.or_chem_objective.restype = ctypes.c_int64
         L.or_chem_objective.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_int, _dp]
@@ -233,6 +239,33 @@ def chem_sens_fd(U, dt, nsub, objective, dT=400.0, rtol=1e-8, atol=1e-15, fd_h=1
     bad = lib().or_chem_sens_fd(_p(U), len(U), float(dt), int(nsub), OBJECTIVES[objective], float(dT), float(rtol),
                                 float(atol), float(fd_h), int(bool(frozen)), int(threads), _p(J), _p(G))
     return J, G, int(bad)
+
+
+class FrozenRun:
+    """Strang steps with given step sizes on a one-level grid whose chemistry calls
+    record their accepted step sizes; replay() re-runs them with those steps frozen
+    (the map a discrete adjoint of the run differentiates).  U: ghosted AoS array."""
+
+    def __init__(self, g, U, dts, rtol=1e-8, atol=1e-15, threads=0):
+        self.g, self.rtol, self.atol, self.threads = g, rtol, atol, threads
+        self.U = np.ascontiguousarray(U, dtype=np.float64).copy()
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        self.h = lib().or_run_record(ctypes.byref(g), _p(self.U), len(d), _p(d), float(rtol), float(atol),
+                                     int(threads))
+        if not self.h:
+            raise RuntimeError("oracle run failed")
+
+    def replay(self, U):
+        V = np.ascontiguousarray(U, dtype=np.float64).copy()
+        if lib().or_run_replay(self.h, ctypes.byref(self.g), _p(V), float(self.rtol), float(self.atol),
+                               int(self.threads)):
+            raise RuntimeError("oracle replay failed")
+        return V
+
+    def close(self):
+        if self.h:
+            lib().or_run_free(self.h)
+            self.h = None
 
 
 def rodas4_circle(y, tend, nsteps):

@@ -1,0 +1,135 @@
+"""Multi-level block AMR stepper (hf_amr_*): BlockAMR::run with max_level > 0.
+
+- Full refinement: with every level-1 block active, level 1 is a one-level run of the
+  fine grid (its ghosts are physical or in place) and level 0 its average: the fine
+  level must equal the one-level stepper's result bit for bit.
+- Partial refinement on a periodic box: reflux, average_down, the leaf-cell chemistry
+  and the regrid's conservative interpolation keep the composite totals.
+- Regrid: the active blocks are the deterministic function of the ErrorEst tags
+  (tagged footprint grown by tag_buffer, proper nesting) restated here in Python.
+- The oblique-detonation wedge (three levels) runs and refines along the shock.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def small_det(nx=32, ny=16, periodic=(0, 1)):
+    from hyperflow_gb300 import workloads as W
+    U, lvd = W.det2d(seed=6, diluent="N2", nx=nx, ny=ny, hot_columns=6)
+    lvd = dict(lvd, periodic=periodic)
+    return U, lvd
+
+
+def coarsen(F):
+    """average_down of a whole level: the four children summed row by row (j, i),
+    (j, i+1), (j+1, i), (j+1, i+1), times 1/4 (AMReX avgdown order)."""
+    return (((F[:, 0::2, 0::2] + F[:, 0::2, 1::2]) + F[:, 1::2, 0::2]) + F[:, 1::2, 1::2]) * 0.25
+
+
+def test_amr_full_refinement_equals_fine_run(gpu):
+    import hyperflow_gb300 as hf
+    U, lvd = small_det()
+    lv = hf.make_level(**lvd)
+    box = (-1.0, 1.0, -1.0, 1.0)  # every cell tagged: level 1 covers the domain
+    amr = hf.AmrStepper(gpu, lv, cuda(U), max_level=1, block=16, tags=dict(box=box, box_only=True))
+    assert amr.info(0)["finest"] == 1
+    F0, act = amr.level(1)
+    assert act.all()
+    fine = hf.make_level(**dict(lvd, nx=2 * lvd["nx"], ny=2 * lvd["ny"], dx=lvd["dx"] / 2, dy=lvd["dy"] / 2))
+    st = hf.Stepper(gpu, fine, F0.contiguous(), flux="plain", chem="batched")
+    for _ in range(4):
+        dt = amr.step(cfl=0.5)
+        assert st.step(dt=dt) == dt
+    F, _ = amr.level(1)
+    assert torch.equal(F, st.state())
+    C, _ = amr.level(0)
+    assert np.array_equal(C.cpu().numpy(), coarsen(F.cpu().numpy()))
+    st.close()
+    amr.close()
+
+
+def test_amr_partial_refinement_conserves(gpu):
+    import hyperflow_gb300 as hf
+    U, lvd = small_det(periodic=(1, 1))
+    lv = hf.make_level(**lvd)
+    x0, x1 = lvd["dx"] * 4, lvd["dx"] * 14  # refine a band over the hot columns and beyond
+    amr = hf.AmrStepper(gpu, lv, cuda(U), max_level=1, block=16, tag_buffer=1, regrid_interval=3,
+                        tags=dict(box=(x0, x1, -1.0, 1.0), box_only=True))
+    _, act = amr.level(1)
+    assert 0 < act.sum() < act.size
+    t0 = amr.totals()
+    ns = U.shape[0] - 3
+    mag = np.abs(U).reshape(U.shape[0], -1).sum(1) * lvd["dx"] * lvd["dy"]
+    for _ in range(7):  # two regrids on the way
+        amr.step(cfl=0.5)
+    t1 = amr.totals()
+    mass0, mass1 = t0[:ns].sum(), t1[:ns].sum()
+    assert abs(mass1 - mass0) <= 1e-13 * mass0
+    for n in (ns, ns + 1, ns + 2):
+        assert abs(t1[n] - t0[n]) <= 1e-12 * mag[n], n
+
+
+def test_amr_regrid_blocks_follow_tags(gpu):
+    import hyperflow_gb300 as hf
+    U, lvd = small_det(nx=64, ny=32)
+    lv = hf.make_level(**lvd)
+    tags = dict(pressure_tag=0.08, temperature_tag=0.08, density_tag=0.05)
+    amr = hf.AmrStepper(gpu, lv, cuda(U), max_level=1, block=16, tag_buffer=2, tags=tags)
+    _, act = amr.level(1)
+    # ErrorEst on the base level (one patch, ghosts filled) and the block rule restated
+    import ctypes
+    ps = hf.PatchSet(U.shape[0], [(0, 0, lvd["nx"] - 1, lvd["ny"] - 1)], device="cuda")
+    ps.interior(0).copy_(cuda(U))
+    gpu.check(gpu.lib.hf_fill_ghosts(gpu.h, ctypes.byref(lv), ps.patches, 1, ctypes.c_void_p(ps.data.data_ptr()),
+                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "fill")
+    t = hf.tag_cells(gpu, lv, ps, 0.0, chemistry=True, **tags).cpu().numpy().reshape(lvd["ny"], lvd["nx"])
+    half, buf = 8, 2
+    nby, nbx = act.shape
+    want = np.zeros_like(act)
+    for bj in range(nby):
+        for bi in range(nbx):
+            i0, j0 = bi * half, bj * half
+            # the footprint grown by tag_buffer: cut at the x edges, wrapped in y (periodic)
+            rows = np.arange(j0 - buf, j0 + half + buf) % lvd["ny"]
+            sub = t[rows][:, max(i0 - buf, 0):min(i0 + half + buf, lvd["nx"])]
+            want[bj, bi] = 1 if sub.any() else 0  # nesting holds: level 0 is all active
+    assert want.any() and not want.all()
+    assert np.array_equal(act, want)
+    amr.close()
+
+
+def test_amr_wedge_three_levels(gpu):
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import workloads as W
+    ctx = gpu
+    U, lvd = W.wedge(nx=64, ny=32)
+    lv = hf.make_level(**lvd)
+    amr = hf.AmrStepper(ctx, lv, cuda(U), max_level=2, block=16, tag_buffer=2, regrid_interval=4,
+                        tags=dict(density_tag=0.05))
+    t = 0.0
+    for _ in range(12):
+        t += amr.step(cfl=0.5)
+    assert abs(amr.time - t) <= 1e-15 * t
+    info = [amr.info(l) for l in range(3)]
+    assert info[0]["finest"] == 2
+    assert info[2]["leaf_cells"] > 0
+    # the refinement follows the shock off the wedge surface: level-1 blocks sit over
+    # the wedge (x >= 0), none far upstream of the tip in the free stream at the top left
+    _, act1 = amr.level(1)
+    assert act1.sum() > 0
+    assert act1[-1, 0] == 0
+    for l in range(3):
+        F, a = amr.level(l)
+        blk = 16
+        for bj, bi in zip(*np.nonzero(a)):
+            Fb = F[:, bj * blk:(bj + 1) * blk, bi * blk:(bi + 1) * blk]
+            assert torch.isfinite(Fb).all()
+            assert (Fb[:9] >= 0).all()
+    amr.close()

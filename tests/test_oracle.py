@@ -240,3 +240,33 @@ def test_sensitivity_fd_frozen_and_adaptive_agree(oracle):
     assert np.max(np.abs(Gf[ok] - Ga[ok]) / scale) < 1e-6
     # H + O2 <=> O + OH dominates and shortens the delay
     assert np.all(np.argmax(np.abs(Gf[ok]), 1) == 0) and np.all(Gf[ok][:, 0] < 0)
+
+
+def test_frozen_run_replay(oracle):
+    # a recorded run of Strang steps replays bit for bit with its chemistry step
+    # sequences frozen, and a rate multiplier changes the replayed result smoothly
+    from hyperflow_gb300 import workloads as W
+    U, lvd = W.det1d(diluent="N2", nx=40)
+    g = oracle.make_grid(40, 2, lvd["dx"], lvd["dy"], periodic=(0, 0), bc_lo=(0, 0), bc_hi=(1, 0), inlet=lvd["inlet"])
+    Ug = oracle.ghosted(U.transpose(1, 2, 0))
+    V, dts = Ug.copy(), []
+    for _ in range(6):
+        dt = oracle.cfl_dt(g, V, 0.5)
+        dts.append(dt)
+        V, dta, st, _ = oracle.strang_step(g, V, dt)
+        assert st == 0 and dta == dt
+    fr = oracle.FrozenRun(g, Ug, dts)
+    try:
+        assert np.array_equal(fr.U[2:-2, 2:-2], V[2:-2, 2:-2])
+        assert np.array_equal(fr.replay(Ug)[2:-2, 2:-2], V[2:-2, 2:-2])
+        m = np.ones(21)
+        m[0] = np.exp(1e-6)
+        oracle.set_rate_mult(m)
+        try:
+            W1 = fr.replay(Ug)[2:-2, 2:-2]
+        finally:
+            oracle.set_rate_mult(None)
+        d = np.abs(W1 - V[2:-2, 2:-2]).max()
+        assert 0 < d < 1e-3 * np.abs(V[2:-2, 2:-2]).max()
+    finally:
+        fr.close()
