@@ -47,6 +47,14 @@ def _need_cuda64(t, name):
         raise TypeError("%s must be a float64 CUDA tensor" % name)
 
 
+def _need_state(ctx, t, name):
+    """A float64 CUDA state whose leading dimension is the context's NV = NS + 3."""
+    _need_cuda64(t, name)
+    if t.dim() < 2 or t.shape[0] != ctx.nv:
+        raise ValueError("%s must have %d components (the mechanism's %d species + 3), got shape %s"
+                         % (name, ctx.nv, ctx.ns, tuple(t.shape)))
+
+
 class Context:
     """hf_init/hf_destroy: one mechanism on one device (src/BlockAMR.cpp:29-30)."""
 
@@ -263,7 +271,10 @@ class ChemistryBatch:
         """field: (NV, n) float64 CUDA tensor (SoA), advanced in place over dt.
 
         Raises RuntimeError("chemistry cell k: ...") on failure; field is unchanged then."""
-        _need_cuda64(field, "field")
+        if cell_index is None:
+            _need_state(self.ctx, field, "field")
+        else:
+            _need_cuda64(field, "field")
         if cell_index is None:
             if not field.is_contiguous():
                 raise ValueError("field must be contiguous (NV, n)")
@@ -405,7 +416,7 @@ class FlowAdjoint:
 
     def __init__(self, ctx, level, U0, nsteps, dts=None, cfl=0.5, checkpoint_every=50, chemistry=True, rtol=1e-8,
                  atol=1e-15):
-        _need_cuda64(U0, "U0")
+        _need_state(ctx, U0, "U0")
         self.ctx = ctx
         U0 = U0.contiguous()
         self.shape = tuple(U0.shape)
@@ -476,7 +487,7 @@ class Stepper:
     (BlockAMR.cpp:409-419).  U0: (NV, ny, nx) float64 CUDA tensor."""
 
     def __init__(self, ctx, level, U0, chemistry=True, rtol=1e-8, atol=1e-15, flux="fused", chem="batched"):
-        _need_cuda64(U0, "U0")
+        _need_state(ctx, U0, "U0")
         self.ctx = ctx
         self.level = level
         self.nv, self.ny, self.nx = U0.shape
@@ -639,7 +650,7 @@ class AmrStepper:
 
     def __init__(self, ctx, level, U0, max_level=1, block=32, tag_buffer=2, regrid_interval=0, chemistry=True,
                  chem="batched", rtol=1e-8, atol=1e-15, tags=None):
-        _need_cuda64(U0, "U0")
+        _need_state(ctx, U0, "U0")
         self.ctx = ctx
         o = L.AmrOpts()
         o.max_level, o.block, o.tag_buffer, o.regrid_interval = int(max_level), int(block), int(tag_buffer), int(

@@ -333,8 +333,8 @@ HF_EXPORT hf_status hf_tag_cells(hf_ctx* ctx, const hf_level* level, const hf_pa
  * combination; react() on the leaf cells; rollback and dt halving.  Regrid every
  * regrid_interval steps (and max_level times at creation): ErrorEst tags (tags) on level l
  * make a level-(l+1) block active when a tagged cell lies in its footprint grown by
- * tag_buffer cells and its footprint grown by 2 cells lies in active level-l blocks; new
- * blocks are filled by ConservativeInterp; the conserved totals are checked to 1e-8 of the
+ * tag_buffer cells and its footprint grown by 2 cells lies in active level-l blocks (both
+ * wrap across periodic edges); new blocks are filled by ConservativeInterp; the conserved totals are checked to 1e-8 of the
  * totals of magnitudes (regridChecked).  base: level 0 (nx, ny multiples of block/2). */
 typedef struct hf_amr_opts {
     int32_t max_level;        /* "max_level" */
