@@ -217,6 +217,7 @@ template <int NS, int D>
 __global__ void __launch_bounds__(128) k_face_plain(Level L, hf_patch P, const double* __restrict__ U,
                                                     double* __restrict__ F, int first_order, int64_t cell_base,
                                                     DevStatus* st) {
+    if (st->abort_run) return;  // an earlier step of this device-resident run failed
     const int fnx = P.nx + (D == 0), fny = P.ny + (D == 1);
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)fnx * fny) return;
@@ -266,10 +267,17 @@ template <int NS>
 __global__ void __launch_bounds__(128) k_update_plain(hf_patch P, const double* __restrict__ Uin,
                                                       const double* __restrict__ Uold, double* __restrict__ Uout,
                                                       const double* __restrict__ Fx, const double* __restrict__ Fy,
-                                                      double cx, double cy, int64_t cell_base, DevStatus* st) {
+                                                      double cx, double cy, const double* __restrict__ hdev,
+                                                      double dx, double dy, int64_t cell_base, DevStatus* st) {
     constexpr int NV = NS + 3;
+    if (st->abort_run) return;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)P.nx * P.ny) return;
+    if (hdev) {  // stage step from device memory (graph-captured steps): h/dx as on the host
+        const double h = *hdev;
+        cx = h / dx;
+        cy = h / dy;
+    }
     const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
     const int64_t nfx = (int64_t)(P.nx + 1) * P.ny, nfy = (int64_t)P.nx * (P.ny + 1);
     const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
@@ -286,22 +294,24 @@ __global__ void __launch_bounds__(128) k_update_plain(hf_patch P, const double* 
 template <int NS>
 static cudaError_t flux_plain_impl(const Level& L, const hf_patch& P, const double* Uin, const double* Uold,
                                    double* Uout, double* fx, double* fy, double h, int first_order,
-                                   int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches) {
+                                   int64_t cell_base, DevStatus* st, cudaStream_t s, int64_t* launches,
+                                   const double* hdev) {
     const int bs = 128;
     const int64_t nfx = (int64_t)(P.nx + 1) * P.ny, nfy = (int64_t)P.nx * (P.ny + 1);
     k_face_plain<NS, 0><<<(unsigned)((nfx + bs - 1) / bs), bs, 0, s>>>(L, P, Uin, fx, first_order, cell_base, st);
     k_face_plain<NS, 1><<<(unsigned)((nfy + bs - 1) / bs), bs, 0, s>>>(L, P, Uin, fy, first_order, cell_base, st);
     const int64_t nc = (int64_t)P.nx * P.ny;
     k_update_plain<NS><<<(unsigned)((nc + bs - 1) / bs), bs, 0, s>>>(P, Uin, Uold, Uout, fx, fy, h / L.dx, h / L.dy,
-                                                                     cell_base, st);
+                                                                     hdev, L.dx, L.dy, cell_base, st);
     *launches += 3;
     return cudaGetLastError();
 }
 cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int, const double* Uin, const double* Uold,
                               double* Uout, double* fx, double* fy, double h, int first_order, int64_t cell_base,
-                              DevStatus* st, cudaStream_t s, int64_t* launches) {
-    return ns == 9 ? flux_plain_impl<9>(L, P, Uin, Uold, Uout, fx, fy, h, first_order, cell_base, st, s, launches)
-                   : flux_plain_impl<10>(L, P, Uin, Uold, Uout, fx, fy, h, first_order, cell_base, st, s, launches);
+                              DevStatus* st, cudaStream_t s, int64_t* launches, const double* hdev) {
+    return ns == 9 ? flux_plain_impl<9>(L, P, Uin, Uold, Uout, fx, fy, h, first_order, cell_base, st, s, launches, hdev)
+                   : flux_plain_impl<10>(L, P, Uin, Uold, Uout, fx, fy, h, first_order, cell_base, st, s, launches,
+                                         hdev);
 }
 
 // ---------------------------------------------------------------- fused form

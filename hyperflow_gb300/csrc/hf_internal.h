@@ -62,10 +62,11 @@ void ctx_add_timing(hf_ctx* ctx, double flux_ms, double chem_ms, double other_ms
 // Launch wrappers (hf_flux.cu)
 cudaError_t launch_fill(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
                         int npatch, double* U, cudaStream_t s, int64_t* launches);
+// hdev (nullable): read the stage length h from device memory instead of the argument
 cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int pidx, const double* Uin,
                               const double* Uold, double* Uout, double* fx, double* fy, double h,
                               int first_order, int64_t cell_base, DevStatus* st, cudaStream_t s,
-                              int64_t* launches);
+                              int64_t* launches, const double* hdev = nullptr);
 // hdev (nullable): read the stage length h from device memory instead of the argument
 cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
                               const double* Uold, double* Uout, double h, const double* hdev, int first_order,

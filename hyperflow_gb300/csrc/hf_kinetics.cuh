@@ -199,9 +199,11 @@ __device__ __forceinline__ void all_rates(const KinCtx<NS>& kc, const double* C,
     (add_rate<(int)Rs, NS>(kc, C, w), ...);
 }
 
-// d(w_i)/dC_m into JC[i][m] (rows i < NS-1), d(w_i)/dT into JT[i].
-template <int R, int NS>
-__device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, double* JC, double* JT) {
+// d(w_i)/dC_m into JC[i][m] (rows i < NS-1), d(w_i)/dT into JT[i]; with W, also the
+// rate of progress into w exactly as add_rate computes it (same k, 1/Kc, products).
+template <int R, int NS, bool W = false>
+__device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, double* JC, double* JT,
+                                        double* w = nullptr) {
     constexpr Reaction rx = RXN[R];
     constexpr int N = NS - 1;
     const double kinf = c_A[R] * arrhenius_T<R>(kc.T, kc.lnT, kc.invT);
@@ -229,6 +231,18 @@ __device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, d
         dkdM = M > 0.0 ? k * dlnk_dlnPr / M : k0 * F;
     }
     const double ikc = inv_kc<R, NS>(kc);
+    if constexpr (W) {
+        double pf = k, pr = k * ikc;
+#pragma unroll
+        for (int i = 0; i < rx.nreac; ++i) pf *= C[rx.reac[i]];
+#pragma unroll
+        for (int i = 0; i < rx.nprod; ++i) pr *= C[rx.prod[i]];
+        const double q = pf - pr;
+#pragma unroll
+        for (int i = 0; i < rx.nreac; ++i) w[rx.reac[i]] -= q;
+#pragma unroll
+        for (int i = 0; i < rx.nprod; ++i) w[rx.prod[i]] += q;
+    }
     double Pf = 1.0, Pb = 1.0;
 #pragma unroll
     for (int i = 0; i < rx.nreac; ++i) Pf *= C[rx.reac[i]];
@@ -292,6 +306,11 @@ template <int NS, size_t... Rs>
 __device__ __forceinline__ void all_jac(const KinCtx<NS>& kc, const double* C, double* JC, double* JT,
                                         std::index_sequence<Rs...>) {
     (add_jac<(int)Rs, NS>(kc, C, JC, JT), ...);
+}
+template <int NS, size_t... Rs>
+__device__ __forceinline__ void all_jac_rates(const KinCtx<NS>& kc, const double* C, double* JC, double* JT,
+                                              double* w, std::index_sequence<Rs...>) {
+    (add_jac<(int)Rs, NS, true>(kc, C, JC, JT, w), ...);
 }
 
 // ---------------------------------------------------------------- ODE pieces
@@ -366,6 +385,50 @@ __device__ __noinline__ bool chem_jac(double rho, double e, double& T, const dou
 #pragma unroll
     for (int j = 0; j < N; ++j) dTdy[j] = -T * ((kc.hRT[j] - 1.0) * INVW.v[j] - eL) / cv;
     const double ir = 1.0 / rho;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const double cl = JC[i * NS + L] * INVW.v[L];
+        const double ti = JT[i] * ir;
+#pragma unroll
+        for (int j = 0; j < N; ++j) J[i * N + j] = D_MW.v[i] * (JC[i * NS + j] * INVW.v[j] - cl + ti * dTdy[j]);
+    }
+    return true;
+}
+
+// chem_rhs and chem_jac at the same y from one temperature solve and one pass over
+// the reactions: dy equals chem_rhs's result (same rate arithmetic, same order) and J
+// chem_jac's.
+template <int NS>
+__device__ __noinline__ bool chem_rhs_jac(double rho, double e, double& T, const double* y, double* dy, double* J) {
+    constexpr int N = NS - 1, L = NS - 1;
+    double z[NS], C[NS], m[6];
+    comp<NS>(y, rho, z, C);
+    double Tn = T;
+    if (!solve_T<NS>(z, e, Tn, m)) return false;
+    T = Tn;
+    KinCtx<NS> kc;
+    kin_setup<NS>(T, C, kc);
+    double JC[N * NS], JT[N], w[NS];
+#pragma unroll
+    for (int i = 0; i < N * NS; ++i) JC[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) JT[i] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) w[k] = 0.0;
+    all_jac_rates<NS>(kc, C, JC, JT, w, std::make_index_sequence<NR>{});
+    bool ok = true;
+    const double ir = 1.0 / rho;
+#pragma unroll
+    for (int k = 0; k < NS - 1; ++k) {
+        dy[k] = w[k] * D_MW.v[k] * ir;
+        ok = ok && isfinite(dy[k]);
+    }
+    if (!ok) return false;
+    const double cv = poly_cv(m, T);
+    double dTdy[N];
+    const double eL = (kc.hRT[L] - 1.0) * INVW.v[L];
+#pragma unroll
+    for (int j = 0; j < N; ++j) dTdy[j] = -T * ((kc.hRT[j] - 1.0) * INVW.v[j] - eL) / cv;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         const double cl = JC[i * NS + L] * INVW.v[L];
@@ -481,7 +544,9 @@ __device__ __noinline__ int cell_begin(ChemCell<NS>& c, const double* u, double 
     c.T = pr.T;
 #pragma unroll
     for (int k = 0; k < N; ++k) c.y[k] = u[k] * ir;
-    if (!chem_rhs<NS>(c.rho, c.e, c.T, c.y, c.f0)) return CELL_FAIL;
+    // f0 and the first step's Jacobian
+    if (!chem_rhs_jac<NS>(c.rho, c.e, c.T, c.y, c.f0, c.J)) return CELL_FAIL;
+    c.Tsave = c.T;
     // starting step: Hairer's estimate in time scaled by the interval
     {
         const double Ts = c.T;
@@ -509,7 +574,7 @@ __device__ __noinline__ int cell_begin(ChemCell<NS>& c, const double* u, double 
     c.steps = 0;
     c.attempts = 0;
     c.rejectLast = c.rejectMore = false;
-    c.needJ = true;
+    c.needJ = false;
     return CELL_CONTINUE;
 }
 
@@ -595,8 +660,10 @@ __device__ __noinline__ int cell_attempt(ChemCell<NS>& c, double rtol, double at
         ++c.steps;
         c.h = hnew;
         if (!(c.t < c.tend)) return CELL_DONE;
-        if (!chem_rhs<NS>(c.rho, c.e, c.T, c.y, c.f0)) return CELL_FAIL;
-        c.needJ = true;
+        if (c.steps >= MAX_STEPS) return CELL_MAXSTEPS;
+        // f0 and the next step's Jacobian at the new y
+        if (!chem_rhs_jac<NS>(c.rho, c.e, c.T, c.y, c.f0, c.J)) return CELL_FAIL;
+        c.Tsave = c.T;
         return CELL_CONTINUE;
     }
     if (c.rejectMore) hnew = c.h * 0.1;
@@ -662,8 +729,7 @@ __device__ __noinline__ int cell_begin_batched(ChemCell<NS>& c, const double* u,
     c.T = pr.T;
 #pragma unroll
     for (int k = 0; k < N; ++k) c.y[k] = u[k] * ir;
-    if (!chem_rhs<NS>(c.rho, c.e, c.T, c.y, c.f0)) return CELL_FAIL;
-    if (!chem_jac<NS>(c.rho, c.e, c.T, c.y, c.J)) return CELL_FAIL;
+    if (!chem_rhs_jac<NS>(c.rho, c.e, c.T, c.y, c.f0, c.J)) return CELL_FAIL;
     c.Tsave = c.T;
     c.t = 0.0;
     c.tend = dt;

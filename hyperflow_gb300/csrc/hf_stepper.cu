@@ -5,9 +5,10 @@
 // by discarding the work buffers (the reference clones the state, :413, :416).
 //
 // Two ways through a step:
-//  * graph path (fused flux + batched chemistry, CFL dt): the whole Strang step -
-//    CFL reduction, dt on the device, four fused Euler stages, ordered batched
-//    chemistry, validation - is one CUDA graph.  Every phase ORs its failure flags
+//  * graph path (batched chemistry, CFL dt): the whole Strang step - CFL reduction,
+//    dt on the device, four Euler stages (fused kernel, or ghost fill + face + update
+//    kernels of the plain form), ordered batched chemistry, validation - is one CUDA
+//    graph.  Every phase ORs its failure flags
 //    into one status block; the host reads it once per step.  Any flag discards the
 //    step and the host-controlled path below re-runs it.
 //  * host-controlled path: the ABI calls one by one with a status read after each,
@@ -61,7 +62,9 @@ struct hf_stepper {
     int* fail = nullptr;
     int32_t* order = nullptr;
     unsigned long long* bins = nullptr;
-    alignas(64) unsigned char tmap[4][128];  // TMA descriptors of the four buffers
+    alignas(64) unsigned char tmap[4][128];  // TMA descriptors of the four buffers (fused form)
+    hf_patch* d_patch = nullptr;             // the level patch in device memory (plain form)
+    double *fx = nullptr, *fy = nullptr;     // face fluxes of one stage (plain form)
     double* base[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t exec[2] = {nullptr, nullptr};  // by which buffer holds the state
     int64_t graph_kernels[2] = {0, 0};             // kernels in each graph
@@ -156,9 +159,17 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     HF_Q(launch_dt_from_rate(st->gst, cfl, st->ddt, s, nl));
     const double* half = st->ddt + 1;
     auto tm = [&](const double* b) { return (const void*)st->tmap[buf_index(st, b)]; };
+    // one Euler stage in -> out (Heun combine with old when non-null), h = dt/2 on the device
+    auto euler = [&](const double* in, const double* old, double* out) -> cudaError_t {
+        if (st->flux_form == HF_FLUX_FUSED)
+            return launch_flux_fused(st->ns, L, P, tm(in), in, old, out, 0.0, half, 0, 0, st->gst, s, nl);
+        cudaError_t q = launch_fill(st->ns, L, &P, st->d_patch, 1, const_cast<double*>(in), s, nl);
+        if (q != cudaSuccess) return q;
+        return launch_flux_plain(st->ns, L, P, 0, in, old, out, st->fx, st->fy, 0.0, 0, 0, st->gst, s, nl, half);
+    };
     // flow(dt/2)
-    HF_Q(launch_flux_fused(st->ns, L, P, tm(S0), S0, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
-    HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, S0, X, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(euler(S0, nullptr, T1));
+    HF_Q(euler(T1, S0, X));
     HF_Q(phase_mark(st, rec, 1, s, nl));
     // react(dt): work-queue head reset, then the ordered batched kernel, commit, validate
     HF_Q(cudaMemsetAsync(&st->gst->counter, 0, sizeof(unsigned long long), s));
@@ -171,8 +182,8 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     }
     HF_Q(phase_mark(st, rec, 2, s, nl));
     // flow(dt/2)
-    HF_Q(launch_flux_fused(st->ns, L, P, tm(X), X, nullptr, T1, 0.0, half, 0, 0, st->gst, s, nl));
-    HF_Q(launch_flux_fused(st->ns, L, P, tm(T1), T1, X, S2, 0.0, half, 0, 0, st->gst, s, nl));
+    HF_Q(euler(X, nullptr, T1));
+    HF_Q(euler(T1, X, S2));
     HF_Q(phase_mark(st, rec, 3, s, nl));
     if (rec) {
         k_run_record<<<1, 1, 0, s>>>(st->gst, st->ddt, rec);
@@ -184,7 +195,7 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
 }
 
 bool graph_ready(const hf_stepper* st) {
-    return st->use_graph && st->flux_form == HF_FLUX_FUSED && (st->chem_form == HF_CHEM_PERSISTENT || !st->chemistry);
+    return st->use_graph && (st->chem_form == HF_CHEM_PERSISTENT || !st->chemistry);
 }
 
 // One step through the graph.  Returns HF_OK with the accepted dt, HF_ERR_INADMISSIBLE
@@ -411,6 +422,13 @@ hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0
     }
     if (ok && flux_form == HF_FLUX_FUSED)
         for (int b = 0; ok && b < 4; ++b) ok = hf::make_tensor_map(st->tmap[b], st->buf[b], P, st->nv);
+    if (ok && flux_form == HF_FLUX_PLAIN) {
+        const size_t fxb = sizeof(double) * st->nv * (size_t)(P.nx + 1) * P.ny;
+        const size_t fyb = sizeof(double) * st->nv * (size_t)P.nx * (P.ny + 1);
+        ok = cudaMalloc(&st->d_patch, sizeof(hf_patch)) == cudaSuccess &&
+             cudaMemcpy(st->d_patch, &P, sizeof(hf_patch), cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMalloc(&st->fx, fxb) == cudaSuccess && cudaMalloc(&st->fy, fyb) == cudaSuccess;
+    }
     if (ok && U0) {
         for (int n = 0; ok && n < st->nv; ++n)
             ok = cudaMemcpy2D(st->buf[0] + n * P.comp_stride + P.ng * P.pitch + P.ng, P.pitch * sizeof(double),
@@ -448,6 +466,9 @@ void hf_stepper_destroy(hf_stepper* st) {
     cudaFree(st->fail);
     cudaFree(st->order);
     cudaFree(st->bins);
+    cudaFree(st->d_patch);
+    cudaFree(st->fx);
+    cudaFree(st->fy);
     delete st;
 }
 
