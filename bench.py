@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--adj1d-cells", type=int, default=1000,
                    help="cells of the 1D detonation whose run is differentiated (0 disables it)")
     p.add_argument("--adj1d-steps", type=int, default=1000, help="CFL Strang steps of that run")
+    p.add_argument("--amr-steps", type=int, default=8,
+                   help="timed steps of the 3-level block-AMR wedge sample (0 disables it)")
     p.add_argument("--nx", type=int, default=NX)
     p.add_argument("--ny", type=int, default=NY)
     return p.parse_args()
@@ -121,13 +123,16 @@ def peaks():
 
 
 # ------------------------------------------------------------------ CPU (oracle) leg
-def cpu_sample(steps=2, warm=1, rows=4, threads=0, nx=NX):
-    """Oracle Strang steps on a periodic strip (nx x rows) of the same workload."""
+def cpu_sample(steps=2, warm=1, rows=4, threads=0, nx=NX, flux_threads=0):
+    """Oracle Strang steps on a periodic strip (nx x rows) of the same workload.
+    flux_threads 1: the reference's serial flux loop; 0: OpenMP over all host threads
+    (same results).  Chemistry always uses OpenMP dynamic,8 over `threads` threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from hyperflow_gb300 import workloads as W
     oracle.build()
     oracle.set_species(10)
+    oracle.set_flux_threads(flux_threads)
     U, lvd = W.det2d(seed=0, diluent="AR", nx=nx, ny=rows)
     g = oracle.make_grid(nx, rows, 1e-4, 1e-4, periodic=(0, 1), bc_lo=(0, 0), bc_hi=(1, 0), inlet=lvd["inlet"])
     Ug = oracle.ghosted(U.transpose(1, 2, 0))
@@ -141,10 +146,12 @@ def cpu_sample(steps=2, warm=1, rows=4, threads=0, nx=NX):
         if st:
             raise RuntimeError("oracle step failed")
     el = time.perf_counter() - t0
+    oracle.set_flux_threads(1)
     cores = threads or os.cpu_count()
+    flux = "serial flux loop (the reference's threading)" if flux_threads == 1 else "OpenMP flux loops"
     return {"value": nx * rows * steps / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
             "sample": "%d Strang steps (after %d warm-up) of a %dx%d periodic strip of the 2D detonation; "
-                      "serial flux loop, OpenMP dynamic,8 chemistry (the reference's threading)" % (steps, warm, nx, rows),
+                      "%s, OpenMP dynamic,8 chemistry" % (steps, warm, nx, rows, flux),
             "seconds": el}
 
 
@@ -152,10 +159,10 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    per = []
-    for _ in range(args.warmup):
-        pass
-    cb = cpu_sample(steps=max(1, args.steps // 4), warm=1, rows=4, nx=args.nx)
+    # a bounded sample: K/4 timed oracle steps after one warm-up step on a 4-row strip,
+    # every loop on all host threads (flux loops included: a stronger baseline than
+    # the reference's serial flux loop, same results)
+    cb = cpu_sample(steps=max(1, args.steps // 4), warm=1, rows=4, nx=args.nx, flux_threads=0)
     line = {"metric": METRIC, "value": cb["value"], "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * args.nx * args.ny / cb["value"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -167,7 +174,6 @@ def run_reference(args):
             "note": "the reference (Cantera/SUNDIALS/AMReX) cannot be built here; this arm times the CPU "
                     "restatement of its path"}
     print(json.dumps(line), flush=True)
-    del per
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -336,6 +342,45 @@ def run_ours(args):
         adjoint["adjoint_over_forward"] = max(v["adjoint_over_forward"] for v in adjoint.values()
                                               if isinstance(v, dict) and "adjoint_over_forward" in v)
 
+    amr = None
+    if args.amr_steps > 0:
+        # bounded sample of the 3-level block-AMR oblique detonation (base 512 x 256,
+        # ratio 2, 32 x 32 blocks, density-gradient tags, regrid every 4 steps): leaf
+        # cell-steps/s over the timed steps; host-driven steps (one status read per
+        # stage), CUDA events around them
+        from hyperflow_gb300 import workloads as W2
+        ctx9a = hf.Context("H2_Li", device=local)
+        Uw, lw = W2.wedge(nx=512, ny=256)
+        amr = {"workload": "oblique detonation over a 30 deg wedge, Mach 7 stoichiometric H2/air at 0.1 atm / 300 K, "
+                           "base 512x256, max_level 2, 32x32 blocks, density tag 0.05, regrid every 4 steps; "
+                           "%d timed steps after %d warm-up steps from the uniform free stream" % (
+                               args.amr_steps, args.warmup)}
+        am = None
+        try:
+            am = hf.AmrStepper(ctx9a, hf.make_level(**lw), torch.from_numpy(Uw).cuda(), max_level=2, block=32,
+                               tag_buffer=2, regrid_interval=4, tags=dict(density_tag=0.05))
+            for _ in range(args.warmup):
+                am.step(cfl=args.cfl)
+            leaf0 = sum(am.info(l)["leaf_cells"] for l in range(3))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            leaf_steps = 0
+            for _ in range(args.amr_steps):
+                leaf_steps += sum(am.info(l)["leaf_cells"] for l in range(3))
+                am.step(cfl=args.cfl)
+            e1.record()
+            torch.cuda.synchronize()
+            ams = e0.elapsed_time(e1)
+            amr.update({"value": leaf_steps / (ams * 1e-3), "unit": "leaf cell-steps/s",
+                        "ms_per_step": ams / args.amr_steps,
+                        "leaf_cells": [am.info(l)["leaf_cells"] for l in range(3)], "leaf_cells_at_start": leaf0})
+        except hf.HyperFlowError as e:  # reported, not fatal to the headline line
+            amr["error"] = str(e)
+        if am is not None:
+            am.close()
+        ctx9a.close()
+
     e2e = None
     if not args.no_e2e:
         st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=args.flux, chem=args.chem)
@@ -381,8 +426,12 @@ def run_ours(args):
                     "the contract, the fp64 object is the binding roof; traffic = ncu dram bytes per launch"}
     cpu = None
     if not args.no_cpu:
-        cb = cpu_sample(steps=4, warm=1, rows=32, nx=args.nx)
+        # all host threads on every loop (the baseline), and the reference's threading
+        # (serial flux loop) beside it
+        cb = cpu_sample(steps=4, warm=1, rows=32, nx=args.nx, flux_threads=0)
+        ca = cpu_sample(steps=2, warm=1, rows=32, nx=args.nx, flux_threads=1)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu["reference_threading"] = {k: ca[k] for k in ("value", "sample")}
     line = {
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -400,7 +449,7 @@ def run_ours(args):
         "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
         "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
         "chem_batch_uneven": chem_batch,
-        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint,
+        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint, "amr": amr,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -80,13 +80,27 @@ __device__ __forceinline__ double third_body(const double* C, double Csum) {
         if (rx.eff[k] != 1.0) M = fma(rx.eff[k] - 1.0, C[k], M);
     return M;
 }
+// log10 of a constant in [0.5, 2] at compile time: 2 atanh((x-1)/(x+1)) / ln 10 by
+// its odd power series (|z| <= 1/3: 40 terms reach the last bit; within 1 ulp of the
+// correctly rounded value for the Troe constants 0.8 and 0.5 of the table).
+constexpr double const_log10(double x) {
+    const double z = (x - 1.0) / (x + 1.0), z2 = z * z;
+    double term = z, sum = 0.0;
+    for (int k = 0; k < 40; ++k) {
+        sum += term / (2 * k + 1);
+        term *= z2;
+    }
+    return 2.0 * sum / 2.302585092994045684;
+}
+
 // Troe: log10 F and its partial derivatives (d log10F/d log10Pr, d log10F/dT).
 template <int R>
 __device__ __forceinline__ double troe_log10F(double T, double Pr, double* dPr, double* dT) {
     constexpr Reaction rx = RXN[R];
     constexpr bool noT3 = rx.troeT3 < 1e-20, noT1 = rx.troeT1 > 1e20;
+    constexpr bool constFcent = noT3 && noT1 && !rx.hasT2;
     double Fcent, dFcent;
-    if constexpr (noT3 && noT1 && !rx.hasT2) {
+    if constexpr (constFcent) {
         Fcent = rx.troeA;
         dFcent = 0.0;
     } else {
@@ -100,7 +114,13 @@ __device__ __forceinline__ double troe_log10F(double T, double Pr, double* dPr, 
         }
     }
     const bool prc = !(Pr > 1e-300);
-    const double lFc = log10(fmax(Fcent, 1e-300));
+    double lFc;
+    if constexpr (constFcent && rx.troeA >= 0.5 && rx.troeA <= 2.0) {
+        constexpr double c = const_log10(rx.troeA);  // F_cent is a constant of the table
+        lFc = c;
+    } else {
+        lFc = log10(fmax(Fcent, 1e-300));
+    }
     const double lPr = log10(fmax(Pr, 1e-300));
     const double c = -0.4 - 0.67 * lFc, nn = 0.75 - 1.27 * lFc;
     const double x = lPr + c, den = nn - 0.14 * x;

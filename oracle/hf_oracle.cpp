@@ -1034,6 +1034,12 @@ void or_fill_ghosts(const or_grid* g, double* U) {
 }
 
 // ---------------------------------------------------------------- Euler stage
+// Threads of the flux, update and validation loops.  1 (default) is the reference's
+// threading (BlockAMR::euler runs its MFIter loops on one thread); more threads give
+// the same results (every face and cell is computed independently).
+static int g_flux_threads = 1;
+extern "C" void or_set_flux_threads(int t) { g_flux_threads = t > 0 ? t : omp_get_max_threads(); }
+
 // BlockAMR.cpp:210-243 on a one-box level.  Ug: ghosted input (ghosts filled).
 // Uout: ghosted output (interior written).  fx: (ny)x(nx+1) faces, fy: (ny+1)x(nx)
 // faces, AoS NV each (may be null).  Returns 0, or 2 when a face's fallback cell
@@ -1048,9 +1054,12 @@ int or_euler_stage(const or_grid* g, const double* Ug, double* Uout, double h, i
     const bool hiWall[2] = {!g->periodic[0] && g->bc_hi[0] == OR_BC_REFLECTING,
                             !g->periodic[1] && g->bc_hi[1] == OR_BC_REFLECTING};
     const bool mixedBottom = !g->periodic[1] && g->bc_lo[1] == OR_BC_WEDGE;
+    const int nt = g_flux_threads;
+    int fail = 0;
     for (int d = 0; d < 2; ++d) {
         const int di = d == 0, dj = d == 1;
         const int fnx = nx + di, fny = ny + dj;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1) reduction(| : fail)
         for (int j = 0; j < fny; ++j) for (int i = 0; i < fnx; ++i) {
             double qa[MAXV], qb[MAXV], qc[MAXV], qd[MAXV], L[MAXV], Rr[MAXV], f[MAXV];
             for (int n = 0; n < nv; ++n) {
@@ -1069,7 +1078,7 @@ int or_euler_stage(const or_grid* g, const double* Ug, double* Uout, double h, i
             if (!properties(Rr, pr)) { std::copy(qc, qc + nv, Rr); }
             // properties() of the fallback states (the reference throws here if even
             // the cell states are inadmissible; ghost-filled valid data never are).
-            if (!properties(L, pl) || !properties(Rr, pr)) return 2;
+            if (!properties(L, pl) || !properties(Rr, pr)) { fail = 1; continue; }
             hllc(L, Rr, d == 0 ? MX() : MY(), pl, pr, f);
             const int coord = d == 0 ? i : j;
             const double x = g->xlo + (i + 0.5) * g->dx;
@@ -1083,7 +1092,9 @@ int or_euler_stage(const or_grid* g, const double* Ug, double* Uout, double h, i
             std::copy(f, f + nv, dst);
         }
     }
+    if (fail) return 2;
     const double cx = h / g->dx, cy = h / g->dy;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
     for (int j = 0; j < ny; ++j) for (int i = 0; i < nx; ++i) {
         const double* fl = &fx[((size_t)j * (nx + 1) + i) * nv];
         const double* fr = fl + nv;
@@ -1130,13 +1141,16 @@ int or_repair_roundoff(const or_grid* g, double* Ug, long* repairs) {
 
 // BlockAMR.cpp:286-298: 0 if every cell is admissible, else 1.
 int or_validate(const or_grid* g, const double* Ug) {
+    const int nt = g_flux_threads;
+    int bad = 0;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1) reduction(| : bad)
     for (int j = 0; j < g->ny; ++j) for (int i = 0; i < g->nx; ++i) {
         double q[MAXV];
         for (int n = 0; n < NV(); ++n) q[n] = atc(g, Ug, i, j, n);
         Props p;
-        if (!properties(q, p)) return 1;
+        if (!properties(q, p)) bad = 1;
     }
-    return 0;
+    return bad;
 }
 
 struct or_stats { long first_order_stages, roundoff_repairs, retries, chem_failures; };

@@ -67,6 +67,7 @@ def lib():
                                     ctypes.c_double, ctypes.c_int, _lp]
         L.or_rodas4_circle.argtypes = [_dp, ctypes.c_double, ctypes.c_int]
         L.or_set_rate_mult.argtypes = [_dp]
+        L.or_set_flux_threads.argtypes = [ctypes.c_int]
         L.or_run_record.restype = ctypes.c_void_p
         L.or_run_record.argtypes = [ctypes.POINTER(Grid), _dp, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int]
@@ -208,6 +209,12 @@ def chem_batch(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
 
 
 OBJECTIVES = {"ignition_delay": 0, "peak_pressure": 1, "final_T": 2}
+
+
+def set_flux_threads(threads=1):
+    """Threads of the flux, update and validation loops (1: the reference's serial
+    loops; 0: all host threads).  Results do not depend on it."""
+    lib().or_set_flux_threads(int(threads))
 
 
 def set_rate_mult(mult=None):

@@ -270,3 +270,23 @@ def test_frozen_run_replay(oracle):
         assert 0 < d < 1e-3 * np.abs(V[2:-2, 2:-2]).max()
     finally:
         fr.close()
+
+
+def test_threaded_flux_loops_bitwise_equal(oracle):
+    # the OpenMP flux/update/validation loops (CPU baseline) give the serial loops' bits
+    from hyperflow_gb300 import workloads as W
+    U, lvd = W.det2d(seed=1, diluent="N2", nx=64, ny=8, hot_columns=8)
+    g = oracle.make_grid(64, 8, lvd["dx"], lvd["dy"], periodic=(0, 1), bc_lo=(0, 0), bc_hi=(1, 0),
+                         inlet=lvd["inlet"])
+    Ug = oracle.ghosted(U.transpose(1, 2, 0))
+    dt = oracle.cfl_dt(g, Ug, 0.5)
+    out = []
+    for ft in (1, 4):
+        oracle.set_flux_threads(ft)
+        try:
+            V, dta, st, _ = oracle.strang_step(g, Ug, dt, chemistry=False)
+        finally:
+            oracle.set_flux_threads(1)
+        assert st == 0
+        out.append(V)
+    assert np.array_equal(out[0], out[1])
