@@ -32,9 +32,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s, 2D H2 detonation FP64: batched vs plain GPU; adjoint/forward time"
-# ncu counts of k_chem_batched (profiles/launches_det2d_2048x512_bench.md): FP64 flops per
-# integrator step attempt, and DRAM bytes (read + write) per launch per cell
-FLOPS_PER_ATTEMPT = 2.15e4
+# ncu counts of k_chem_batched on the 512 x 128 case (profiles/k_chem_batched_det2d_512x128.md):
+# FP64 flops per integrator step attempt (DFMA x 2 + DADD + DMUL thread instructions of
+# the fourth chemistry launch over its 1.322e6 attempts), and DRAM bytes per launch per cell
+FLOPS_PER_ATTEMPT = 1.87e4
 TRAFFIC_PER_CELL = None
 NX, NY = 2048, 512
 
@@ -63,6 +64,8 @@ def parse():
     p.add_argument("--adj1d-cells", type=int, default=1000,
                    help="cells of the 1D detonation whose run is differentiated (0 disables it)")
     p.add_argument("--adj1d-steps", type=int, default=1000, help="CFL Strang steps of that run")
+    p.add_argument("--det1d-steps", type=int, default=100,
+                   help="timed steps of the 1D detonation sample, 2000 x 2 cells (0 disables it)")
     p.add_argument("--amr-steps", type=int, default=8,
                    help="timed steps of the 3-level block-AMR wedge sample (0 disables it)")
     p.add_argument("--nx", type=int, default=NX)
@@ -342,6 +345,28 @@ def run_ours(args):
         adjoint["adjoint_over_forward"] = max(v["adjoint_over_forward"] for v in adjoint.values()
                                               if isinstance(v, dict) and "adjoint_over_forward" in v)
 
+    det1d = None
+    if args.det1d_steps > 0:
+        # bounded sample of the 1D planar detonation (2000 x 2 cells on 0.1 m, 20-cell
+        # driver at 40 atm / 3000 K, Ar diluent): the same graph-captured steps as the
+        # headline run; few stiff cells, so one cell's chemistry sets the step time
+        U1, l1 = W.det1d(diluent="AR", nx=2000)
+        s1 = hf.Stepper(ctx, hf.make_level(**l1), torch.from_numpy(U1).cuda(), flux=args.flux, chem=args.chem)
+        for _ in range(args.warmup):
+            s1.step(cfl=args.cfl)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        done1 = s1.run(args.det1d_steps, cfl=args.cfl)
+        e1.record()
+        torch.cuda.synchronize()
+        ms1 = e0.elapsed_time(e1)
+        det1d = {"workload": "1D H2/O2/Ar detonation 2000x2 cells on 0.1 m, 20-cell driver at 40 atm/3000 K, "
+                             "reflecting left/top/bottom, transmissive right, CFL %.2f; %d device-resident steps after "
+                             "%d warm-up steps" % (args.cfl, done1, args.warmup),
+                 "value": 4000 * done1 / (ms1 * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms1 / max(done1, 1)}
+        s1.close()
+
     amr = None
     if args.amr_steps > 0:
         # bounded sample of the 3-level block-AMR oblique detonation (base 512 x 256,
@@ -449,7 +474,7 @@ def run_ours(args):
         "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
         "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
         "chem_batch_uneven": chem_batch,
-        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint, "amr": amr,
+        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint, "det1d": det1d, "amr": amr,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -460,7 +460,7 @@ __device__ __forceinline__ void lu_solve_T(const double* A, const int* piv, doub
     for (int i = 0; i < N; ++i) {
 #pragma unroll
         for (int j = 0; j < i; ++j) b[i] = fma(-A[j * N + i], b[j], b[i]);
-        b[i] /= A[i * N + i];
+        b[i] *= A[i * N + i];  // lu_factor stores the reciprocal pivots
     }
 #pragma unroll
     for (int i = N - 2; i >= 0; --i)

@@ -488,6 +488,7 @@ __device__ __forceinline__ double wrms(const double* v, const double* y0, const 
     return fmax(sqrt(s * (1.0 / N)), 1e-10);
 }
 
+// LU with partial pivoting in place (P A = L U); the diagonal holds 1/U_kk.
 template <int N>
 __device__ __forceinline__ bool lu_factor(double* A, int* piv) {
 #pragma unroll
@@ -510,6 +511,7 @@ __device__ __forceinline__ bool lu_factor(double* A, int* piv) {
                 }
         }
         const double inv = 1.0 / A[k * N + k];
+        A[k * N + k] = inv;  // the solves multiply by the reciprocal pivot
 #pragma unroll
         for (int i = k + 1; i < N; ++i) {
             const double l = A[i * N + k] * inv;
@@ -539,7 +541,7 @@ __device__ __forceinline__ void lu_solve(const double* A, const int* piv, double
     for (int i = N - 1; i >= 0; --i) {
 #pragma unroll
         for (int j = i + 1; j < N; ++j) b[i] = fma(-A[i * N + j], b[j], b[i]);
-        b[i] /= A[i * N + i];
+        b[i] *= A[i * N + i];  // reciprocal pivot
     }
 }
 

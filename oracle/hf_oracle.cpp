@@ -408,7 +408,8 @@ bool chem_jac(ChemCell& c, const double* y, double* J) {
     return true;
 }
 
-// LU with partial pivoting, in place; returns false for a singular matrix.
+// LU with partial pivoting, in place (P A = L U, the diagonal holding 1/U_kk, which the
+// solves multiply by); returns false for a singular matrix.
 bool lu_factor(double* A, int* piv, int n) {
     for (int k = 0; k < n; ++k) {
         int p = k;
@@ -418,6 +419,7 @@ bool lu_factor(double* A, int* piv, int n) {
         piv[k] = p;
         if (p != k) for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[p * n + j]);
         const double inv = 1.0 / A[k * n + k];
+        A[k * n + k] = inv;
         for (int i = k + 1; i < n; ++i) {
             const double l = A[i * n + k] * inv;
             A[i * n + k] = l;
@@ -431,7 +433,7 @@ void lu_solve(const double* A, const int* piv, double* b, int n) {
     for (int i = 1; i < n; ++i) for (int j = 0; j < i; ++j) b[i] -= A[i * n + j] * b[j];
     for (int i = n - 1; i >= 0; --i) {
         for (int j = i + 1; j < n; ++j) b[i] -= A[i * n + j] * b[j];
-        b[i] /= A[i * n + i];
+        b[i] *= A[i * n + i];
     }
 }
 
