@@ -35,7 +35,7 @@ METRIC = "cell-steps/s, 2D H2 detonation FP64: batched vs plain GPU; adjoint/for
 # ncu counts of k_chem_batched on the 512 x 128 case (profiles/k_chem_batched_det2d_512x128.md):
 # FP64 flops per integrator step attempt (DFMA x 2 + DADD + DMUL thread instructions of
 # the fourth chemistry launch over its 1.322e6 attempts), and DRAM bytes per launch per cell
-FLOPS_PER_ATTEMPT = 1.87e4
+FLOPS_PER_ATTEMPT = 1.79e4
 TRAFFIC_PER_CELL = None
 NX, NY = 2048, 512
 

@@ -26,6 +26,8 @@ struct hf_ctx {
     size_t scratch_bytes = 0;
     hf_patch* d_patches = nullptr;
     int d_patch_cap = 0;
+    int64_t* d_off = nullptr;  // per-patch offsets of the multi-patch flux launches
+    int d_off_cap = 0;
     // tensor-map cache for the fused flux kernel
     struct TMap { const double* base; hf_patch P; alignas(64) unsigned char map[128]; };
     std::vector<TMap> tmaps;
@@ -109,6 +111,18 @@ cudaError_t upload_patches(hf_ctx* ctx, const hf_patch* p, int n, cudaStream_t s
         ctx->d_patch_cap = n;
     }
     cudaError_t e = cudaMemcpyAsync(ctx->d_patches, p, sizeof(hf_patch) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+static cudaError_t upload_offsets(hf_ctx* ctx, const int64_t* v, int n, cudaStream_t s) {
+    if (n > ctx->d_off_cap) {
+        if (ctx->d_off) cudaFree(ctx->d_off);
+        ctx->d_off = nullptr;
+        cudaError_t e = cudaMalloc(&ctx->d_off, sizeof(int64_t) * n);
+        if (e != cudaSuccess) return e;
+        ctx->d_off_cap = n;
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->d_off, v, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(s);
 }
@@ -218,6 +232,7 @@ void hf_destroy(hf_ctx* ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->d_patches) cudaFree(ctx->d_patches);
+    if (ctx->d_off) cudaFree(ctx->d_off);
     delete ctx;
 }
 
@@ -357,16 +372,26 @@ hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* pat
             if (!tm) return fail(ctx, HF_ERR_ARG, "flux_update: TMA descriptor rejected (alignment/pitch)");
             HF_CUDA(launch_flux_fused(ctx->ns, L, patches[0], tm, U_in, uold, U_out, h, nullptr, first_order, 0, ctx->st, s,
                                       &ctx->cnt.kernel_launches));
+        } else if (npatch == 1) {
+            HF_CUDA(launch_flux_plain(ctx->ns, L, patches[0], 0, U_in, uold, U_out, FX, FY, h, first_order, 0, ctx->st,
+                                      s, &ctx->cnt.kernel_launches));
         } else {
+            // every patch in one launch per kernel: face arrays packed per patch in patch order
+            std::vector<int64_t> off(3 * (size_t)npatch);
             int64_t base = 0, ox = 0, oy = 0;
             for (int p = 0; p < npatch; ++p) {
                 const hf_patch& P = patches[p];
-                HF_CUDA(launch_flux_plain(ctx->ns, L, P, p, U_in, uold, U_out, FX + ox, FY + oy, h, first_order, base,
-                                          ctx->st, s, &ctx->cnt.kernel_launches));
+                off[3 * p] = ox;
+                off[3 * p + 1] = oy;
+                off[3 * p + 2] = base;
                 base += (int64_t)P.nx * P.ny;
                 ox += (int64_t)nv * (P.nx + 1) * P.ny;
                 oy += (int64_t)nv * P.nx * (P.ny + 1);
             }
+            HF_CUDA(upload_patches(ctx, patches, npatch, s));
+            HF_CUDA(upload_offsets(ctx, off.data(), 3 * npatch, s));
+            HF_CUDA(launch_flux_multi(ctx->ns, L, patches, ctx->d_patches, npatch, ctx->d_off, U_in, uold, U_out, FX, FY,
+                                      h, first_order, ctx->st, s, &ctx->cnt.kernel_launches));
         }
         toc(ctx, s, ctx->cnt.kernel_launches - l0);
         HF_CUDA(read_status(ctx, s));

@@ -41,7 +41,12 @@ struct AmrLevel {
     hf_patch dom{};                 // the whole level domain as one patch view
     int nbx = 0, nby = 0;
     std::vector<uint8_t> active;    // [nby][nbx]
-    std::vector<hf_patch> patches;  // active blocks, row-major block order
+    std::vector<hf_patch> blocks;   // active blocks, row-major block order
+    std::vector<hf_patch> patches;  // the patches of the ABI calls: the blocks, or the
+                                    // domain as one patch when every block is active
+    int32_t* d_regions = nullptr;   // coarse-fine ghost regions (4 int32 each, device)
+    int nregions = 0;
+    int64_t region_cells = 1;       // largest coarsened region
     size_t bytes = 0;
     double *U = nullptr, *S = nullptr, *N = nullptr, *O = nullptr, *B = nullptr;  // state, stage, next, old, backup
     double *fx = nullptr, *fy = nullptr;  // face fluxes packed per patch (capacity: every block)
@@ -82,16 +87,28 @@ hf_patch block_patch(const AmrLevel& a, int bi, int bj, int B) {
     return p;
 }
 
-// Rebuilds patches, leaf lists and leaf masks of every level from the active maps.
+hf_status cf_regions(hf_amr* m, int l, cudaStream_t s);
+
+// Rebuilds blocks, patches, leaf lists, leaf masks and coarse-fine ghost regions of
+// every level from the active maps.
 hf_status rebuild(hf_amr* m, cudaStream_t s) {
     const int B = m->o.block;
     for (int l = 0; l <= m->o.max_level; ++l) {
         AmrLevel& a = m->lev[l];
-        a.patches.clear();
+        a.blocks.clear();
         if (l <= m->finest)
             for (int bj = 0; bj < a.nby; ++bj)
                 for (int bi = 0; bi < a.nbx; ++bi)
-                    if (a.active[(size_t)bj * a.nbx + bi]) a.patches.push_back(block_patch(a, bi, bj, B));
+                    if (a.active[(size_t)bj * a.nbx + bi]) a.blocks.push_back(block_patch(a, bi, bj, B));
+        // a fully active level runs as one patch: 3 flux launches instead of 3 per block
+        if (!a.blocks.empty() && a.blocks.size() == a.active.size())
+            a.patches.assign(1, a.dom);
+        else
+            a.patches = a.blocks;
+    }
+    for (int l = 1; l <= m->finest; ++l) {
+        hf_status r = cf_regions(m, l, s);
+        if (r != HF_OK) return r;
     }
     for (int l = 0; l <= m->finest; ++l) {
         AmrLevel& a = m->lev[l];
@@ -130,16 +147,19 @@ int wrap_cell(int g, int n, int periodic) {
     return periodic ? ((g % n) + n) % n : -1;
 }
 
-// Coarse-fine ghosts of level l's blocks: the 2-cell frame parts that lie in inactive
-// blocks (across a periodic boundary: the inactive periodic image), by
-// ConservativeInterp from level l-1.  A frame part outside a non-periodic domain
-// edge holds physical ghosts.  Across a periodic edge the region is interpolated in
-// place from the coarse level's ghost frame, which holds the periodic image.
-hf_status fill_cf(hf_amr* m, int l, double* Uf, const double* Uc, cudaStream_t s) {
-    const AmrLevel& a = m->lev[l];
+// Coarse-fine ghost regions of level l's blocks: the 2-cell frame parts that lie in
+// inactive blocks (across a periodic boundary: the inactive periodic image), filled by
+// ConservativeInterp from level l-1.  A frame part outside a non-periodic domain edge
+// holds physical ghosts.  Across a periodic edge the region is interpolated in place
+// from the coarse level's ghost frame, which holds the periodic image.  Regions are in
+// level-l indices of the dense level array; uploaded once per rebuild.
+hf_status cf_regions(hf_amr* m, int l, cudaStream_t s) {
+    AmrLevel& a = m->lev[l];
     const AmrLevel& c = m->lev[l - 1];
     const int B = m->o.block;
-    for (const hf_patch& p : a.patches) {
+    std::vector<int32_t> reg;
+    int64_t cells = 1;
+    for (const hf_patch& p : a.blocks) {
         const int bi = p.ilo / B, bj = p.jlo / B;
         for (int dj = -1; dj <= 1; ++dj)
             for (int di = -1; di <= 1; ++di) {
@@ -153,10 +173,33 @@ hf_status fill_cf(hf_amr* m, int l, double* Uf, const double* Uc, cudaStream_t s
                 r[2] = di < 0 ? p.ilo - 1 : (di > 0 ? p.ilo + p.nx + 1 : p.ilo + p.nx - 1);
                 r[1] = dj < 0 ? p.jlo - 2 : (dj > 0 ? p.jlo + p.ny : p.jlo);
                 r[3] = dj < 0 ? p.jlo - 1 : (dj > 0 ? p.jlo + p.ny + 1 : p.jlo + p.ny - 1);
-                hf_status q = hf_interp_coarse_to_fine(m->ctx, &c.dom, Uc, &p, Uf, r, s);
-                if (q != HF_OK) return q;
+                // inside the fine array's ghosted box; the coarsened box grown by one
+                // inside the coarse array's ghosted box
+                if (r[0] < -2 || r[1] < -2 || r[2] > a.L.nx + 1 || r[3] > a.L.ny + 1 || (r[0] >> 1) - 1 < -2 ||
+                    (r[1] >> 1) - 1 < -2 || (r[2] >> 1) + 1 > c.L.nx + 1 || (r[3] >> 1) + 1 > c.L.ny + 1)
+                    return HF_ERR_ARG;
+                reg.insert(reg.end(), r, r + 4);
+                cells = std::max<int64_t>(cells, (int64_t)((r[2] >> 1) - (r[0] >> 1) + 1) * ((r[3] >> 1) - (r[1] >> 1) + 1));
             }
     }
+    a.nregions = (int)(reg.size() / 4);
+    a.region_cells = cells;
+    if (reg.empty()) return HF_OK;
+    return cuda_st(cudaMemcpyAsync(a.d_regions, reg.data(), sizeof(int32_t) * reg.size(), cudaMemcpyHostToDevice, s)) ==
+                   HF_OK
+               ? cuda_st(cudaStreamSynchronize(s))
+               : HF_ERR_CUDA;
+}
+
+// Coarse-fine ghosts of level l in X[l] from X[l-1]: every region in one launch.
+hf_status fill_cf(hf_amr* m, int l, double* Uf, const double* Uc, cudaStream_t s) {
+    const AmrLevel& a = m->lev[l];
+    const AmrLevel& c = m->lev[l - 1];
+    int64_t nl = 0;
+    if (hf::launch_interp_regions(m->ns, c.dom, Uc, a.dom, Uf, a.d_regions, a.nregions, a.region_cells, s, &nl) !=
+        cudaSuccess)
+        return HF_ERR_CUDA;
+    hf::ctx_add_launches(m->ctx, nl, 0, 0);
     return HF_OK;
 }
 
@@ -421,7 +464,8 @@ hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, con
         ok = ok && cudaMalloc(&a.fx, fb) == cudaSuccess && cudaMalloc(&a.fy, gb) == cudaSuccess &&
              cudaMalloc(&a.cells, sizeof(int64_t) * nc) == cudaSuccess && cudaMalloc(&a.leaf_mask, nc) == cudaSuccess &&
              cudaMalloc(&a.hist.h, sizeof(double) * nc) == cudaSuccess &&
-             cudaMalloc(&a.hist.cost, sizeof(int32_t) * nc) == cudaSuccess;
+             cudaMalloc(&a.hist.cost, sizeof(int32_t) * nc) == cudaSuccess &&
+             cudaMalloc(&a.d_regions, sizeof(int32_t) * 4 * 8 * (size_t)a.nbx * a.nby) == cudaSuccess;
     }
     if (ok) {
         AmrLevel& a = m->lev[0];
@@ -451,6 +495,7 @@ void hf_amr_destroy(hf_amr* m) {
         cudaFree(a.leaf_mask);
         cudaFree(a.hist.h);
         cudaFree(a.hist.cost);
+        cudaFree(a.d_regions);
     }
     delete m;
 }

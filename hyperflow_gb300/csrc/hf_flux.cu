@@ -213,13 +213,12 @@ __device__ __forceinline__ bool face_flux(const Level& L, int gi, int gj, int fi
 }
 
 // ---------------------------------------------------------------- plain form
+// Face idx of direction D of patch P into F (component stride = the patch's face count).
 template <int NS, int D>
-__global__ void __launch_bounds__(128) k_face_plain(Level L, hf_patch P, const double* __restrict__ U,
-                                                    double* __restrict__ F, int first_order, int64_t cell_base,
-                                                    DevStatus* st) {
-    if (st->abort_run) return;  // an earlier step of this device-resident run failed
+__device__ __forceinline__ void face_one(const Level& L, const hf_patch& P, const double* __restrict__ U,
+                                         double* __restrict__ F, int first_order, int64_t cell_base, DevStatus* st,
+                                         int64_t idx) {
     const int fnx = P.nx + (D == 0), fny = P.ny + (D == 1);
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)fnx * fny) return;
     const int fi = (int)(idx % fnx), fj = (int)(idx / fnx);
     PView v{U, P};
@@ -235,6 +234,26 @@ __global__ void __launch_bounds__(128) k_face_plain(Level L, hf_patch P, const d
     const int64_t nf = (int64_t)fnx * fny;
 #pragma unroll
     for (int n = 0; n < NS + 3; ++n) F[n * nf + idx] = f[n];
+}
+
+template <int NS, int D>
+__global__ void __launch_bounds__(128) k_face_plain(Level L, hf_patch P, const double* __restrict__ U,
+                                                    double* __restrict__ F, int first_order, int64_t cell_base,
+                                                    DevStatus* st) {
+    if (st->abort_run) return;  // an earlier step of this device-resident run failed
+    face_one<NS, D>(L, P, U, F, first_order, cell_base, st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// All patches of a level in one launch: patch blockIdx.y, its x/y face arrays at
+// off[3p], off[3p+1] of FX/FY and its first cell's index at off[3p+2].
+template <int NS, int D>
+__global__ void __launch_bounds__(128) k_face_multi(Level L, const hf_patch* __restrict__ patches,
+                                                    const int64_t* __restrict__ off, const double* __restrict__ U,
+                                                    double* __restrict__ F, int first_order, DevStatus* st) {
+    const int p = blockIdx.y;
+    const hf_patch P = patches[p];
+    face_one<NS, D>(L, P, U, F + off[3 * p + D], first_order, off[3 * p + 2], st,
+                    (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Validation of an updated cell, then optional Heun combine.  Negative partial
@@ -263,21 +282,14 @@ __device__ __forceinline__ void finish_cell(double* q, const double* __restrict_
     for (int n = 0; n < NV; ++n) Uout[gidx + n * cstride] = q[n];
 }
 
+// Update, validation and optional Heun combine of cell idx of patch P.
 template <int NS>
-__global__ void __launch_bounds__(128) k_update_plain(hf_patch P, const double* __restrict__ Uin,
-                                                      const double* __restrict__ Uold, double* __restrict__ Uout,
-                                                      const double* __restrict__ Fx, const double* __restrict__ Fy,
-                                                      double cx, double cy, const double* __restrict__ hdev,
-                                                      double dx, double dy, int64_t cell_base, DevStatus* st) {
+__device__ __forceinline__ void update_one(const hf_patch& P, const double* __restrict__ Uin,
+                                           const double* __restrict__ Uold, double* __restrict__ Uout,
+                                           const double* __restrict__ Fx, const double* __restrict__ Fy, double cx,
+                                           double cy, int64_t cell_base, DevStatus* st, int64_t idx) {
     constexpr int NV = NS + 3;
-    if (st->abort_run) return;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)P.nx * P.ny) return;
-    if (hdev) {  // stage step from device memory (graph-captured steps): h/dx as on the host
-        const double h = *hdev;
-        cx = h / dx;
-        cy = h / dy;
-    }
     const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
     const int64_t nfx = (int64_t)(P.nx + 1) * P.ny, nfy = (int64_t)P.nx * (P.ny + 1);
     const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
@@ -289,6 +301,33 @@ __global__ void __launch_bounds__(128) k_update_plain(hf_patch P, const double* 
         q[n] = Uin[g + n * P.comp_stride] - cx * (fr - fl) - cy * (ft - fb);
     }
     finish_cell<NS>(q, Uold, g, P.comp_stride, Uout, cell_base + idx, st);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(128) k_update_plain(hf_patch P, const double* __restrict__ Uin,
+                                                      const double* __restrict__ Uold, double* __restrict__ Uout,
+                                                      const double* __restrict__ Fx, const double* __restrict__ Fy,
+                                                      double cx, double cy, const double* __restrict__ hdev,
+                                                      double dx, double dy, int64_t cell_base, DevStatus* st) {
+    if (st->abort_run) return;
+    if (hdev) {  // stage step from device memory (graph-captured steps): h/dx as on the host
+        const double h = *hdev;
+        cx = h / dx;
+        cy = h / dy;
+    }
+    update_one<NS>(P, Uin, Uold, Uout, Fx, Fy, cx, cy, cell_base, st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(128) k_update_multi(const hf_patch* __restrict__ patches,
+                                                      const int64_t* __restrict__ off, const double* __restrict__ Uin,
+                                                      const double* __restrict__ Uold, double* __restrict__ Uout,
+                                                      const double* __restrict__ FX, const double* __restrict__ FY,
+                                                      double cx, double cy, DevStatus* st) {
+    const int p = blockIdx.y;
+    const hf_patch P = patches[p];
+    update_one<NS>(P, Uin, Uold, Uout, FX + off[3 * p], FY + off[3 * p + 1], cx, cy, off[3 * p + 2], st,
+                   (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <int NS>
@@ -305,6 +344,36 @@ static cudaError_t flux_plain_impl(const Level& L, const hf_patch& P, const doub
                                                                      hdev, L.dx, L.dy, cell_base, st);
     *launches += 3;
     return cudaGetLastError();
+}
+template <int NS>
+static cudaError_t flux_multi_impl(const Level& L, const hf_patch* ph, const hf_patch* pd, int npatch,
+                                   const int64_t* offd, const double* Uin, const double* Uold, double* Uout,
+                                   double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
+                                   int64_t* launches) {
+    const int bs = 128;
+    int64_t mfx = 1, mfy = 1, mc = 1;
+    for (int p = 0; p < npatch; ++p) {
+        mfx = max(mfx, (int64_t)(ph[p].nx + 1) * ph[p].ny);
+        mfy = max(mfy, (int64_t)ph[p].nx * (ph[p].ny + 1));
+        mc = max(mc, (int64_t)ph[p].nx * ph[p].ny);
+    }
+    k_face_multi<NS, 0><<<dim3((unsigned)((mfx + bs - 1) / bs), (unsigned)npatch), bs, 0, s>>>(L, pd, offd, Uin, FX,
+                                                                                             first_order, st);
+    k_face_multi<NS, 1><<<dim3((unsigned)((mfy + bs - 1) / bs), (unsigned)npatch), bs, 0, s>>>(L, pd, offd, Uin, FY,
+                                                                                             first_order, st);
+    k_update_multi<NS><<<dim3((unsigned)((mc + bs - 1) / bs), (unsigned)npatch), bs, 0, s>>>(
+        pd, offd, Uin, Uold, Uout, FX, FY, h / L.dx, h / L.dy, st);
+    *launches += 3;
+    return cudaGetLastError();
+}
+cudaError_t launch_flux_multi(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
+                              int npatch, const int64_t* off_dev, const double* Uin, const double* Uold, double* Uout,
+                              double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
+                              int64_t* launches) {
+    return ns == 9 ? flux_multi_impl<9>(L, patches_host, patches_dev, npatch, off_dev, Uin, Uold, Uout, FX, FY, h,
+                                        first_order, st, s, launches)
+                   : flux_multi_impl<10>(L, patches_host, patches_dev, npatch, off_dev, Uin, Uold, Uout, FX, FY, h,
+                                         first_order, st, s, launches);
 }
 cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int, const double* Uin, const double* Uold,
                               double* Uout, double* fx, double* fy, double h, int first_order, int64_t cell_base,
@@ -785,13 +854,13 @@ cudaError_t launch_hllc(int ns, const double* l, const double* r, const double* 
 // region; one common minmod slope pair for all components, theta halved (<= 48
 // times) until all four children are admissible, theta = 0 otherwise.
 template <int NS>
-__global__ void k_interp(hf_patch C, const double* __restrict__ Uc, hf_patch F, double* __restrict__ Uf, int rfi0,
-                         int rfj0, int rfi1, int rfj1) {
+__device__ __forceinline__ void interp_one(const hf_patch& C, const double* __restrict__ Uc, const hf_patch& F,
+                                           double* __restrict__ Uf, int rfi0, int rfj0, int rfi1, int rfj1,
+                                           int64_t idx) {
     constexpr int NV = NS + 3;
     // coarse index box of the region
     const int ci0 = rfi0 >> 1, cj0 = rfj0 >> 1, ci1 = rfi1 >> 1, cj1 = rfj1 >> 1;
     const int cnx = ci1 - ci0 + 1, cny = cj1 - cj0 + 1;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)cnx * cny) return;
     const int ci = ci0 + (int)(idx % cnx), cj = cj0 + (int)(idx / cnx);
     auto rd = [&](int gi, int gj, int n) {
@@ -829,6 +898,28 @@ __global__ void k_interp(hf_patch C, const double* __restrict__ Uc, hf_patch F, 
                 Uf[F.offset + (int64_t)n * F.comp_stride + (int64_t)(fj - F.jlo + F.ng) * F.pitch + (fi - F.ilo + F.ng)] =
                     q[n] + theta * ((a ? 0.25 : -0.25) * sx[n] + (b ? 0.25 : -0.25) * sy[n]);
         }
+}
+template <int NS>
+__global__ void k_interp(hf_patch C, const double* __restrict__ Uc, hf_patch F, double* __restrict__ Uf, int rfi0,
+                         int rfj0, int rfi1, int rfj1) {
+    interp_one<NS>(C, Uc, F, Uf, rfi0, rfj0, rfi1, rfj1, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+// Many regions of one fine patch from one coarse patch: region blockIdx.y is
+// regions[4r .. 4r+3] = (i0, j0, i1, j1) in fine level indices.
+template <int NS>
+__global__ void k_interp_regions(hf_patch C, const double* __restrict__ Uc, hf_patch F, double* __restrict__ Uf,
+                                 const int32_t* __restrict__ regions) {
+    const int32_t* r = regions + 4 * (int64_t)blockIdx.y;
+    interp_one<NS>(C, Uc, F, Uf, r[0], r[1], r[2], r[3], (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+cudaError_t launch_interp_regions(int ns, const hf_patch& C, const double* Uc, const hf_patch& F, double* Uf,
+                                  const int32_t* regions_dev, int nregions, int64_t max_coarse_cells, cudaStream_t s,
+                                  int64_t* launches) {
+    if (nregions <= 0) return cudaSuccess;
+    const dim3 grid((unsigned)((max_coarse_cells + 127) / 128), (unsigned)nregions);
+    HF_DISPATCH(ns, k_interp_regions)<<<grid, 128, 0, s>>>(C, Uc, F, Uf, regions_dev);
+    ++*launches;
+    return cudaGetLastError();
 }
 cudaError_t launch_interp(int ns, const hf_patch& C, const double* Uc, const hf_patch& F, double* Uf,
                           const int32_t* r, cudaStream_t s, int64_t* launches) {

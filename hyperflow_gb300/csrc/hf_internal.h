@@ -67,6 +67,13 @@ cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int pid
                               const double* Uold, double* Uout, double* fx, double* fy, double h,
                               int first_order, int64_t cell_base, DevStatus* st, cudaStream_t s,
                               int64_t* launches, const double* hdev = nullptr);
+// The plain form over all patches of a level in 3 launches; off_dev[3p..3p+2] = patch p's
+// x-face offset in FX, y-face offset in FY and first cell index (face arrays packed per
+// patch, component-major within a patch, as launch_flux_plain writes them).
+cudaError_t launch_flux_multi(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
+                              int npatch, const int64_t* off_dev, const double* Uin, const double* Uold, double* Uout,
+                              double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
+                              int64_t* launches);
 // hdev (nullable): read the stage length h from device memory instead of the argument
 cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
                               const double* Uold, double* Uout, double h, const double* hdev, int first_order,
@@ -89,6 +96,11 @@ cudaError_t launch_properties(int ns, const double* q, int64_t stride, int64_t c
                               double* T, int32_t* status, DevStatus* st, cudaStream_t s, int64_t* launches);
 cudaError_t launch_hllc(int ns, const double* l, const double* r, const double* pl, const double* pr,
                         int64_t stride, int64_t count, int dir, double* f, cudaStream_t s, int64_t* launches);
+// Regions (4 int32 each, fine level indices, in device memory) of one fine patch from one
+// coarse patch, one launch; max_coarse_cells bounds each region's coarsened box.
+cudaError_t launch_interp_regions(int ns, const hf_patch& C, const double* Uc, const hf_patch& F, double* Uf,
+                                  const int32_t* regions_dev, int nregions, int64_t max_coarse_cells, cudaStream_t s,
+                                  int64_t* launches);
 cudaError_t launch_interp(int ns, const hf_patch& C, const double* Uc, const hf_patch& F, double* Uf,
                           const int32_t* region, cudaStream_t s, int64_t* launches);
 
