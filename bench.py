@@ -77,6 +77,22 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(dist, x, device):
+    """The largest x over the ranks of the process group (x itself without one)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, units_per_rank, steps, slowest_ms):
+    """Whole-job throughput of `world` independent replicas: all ranks' units over the
+    slowest rank's time (units per second)."""
+    return world * units_per_rank * steps / (slowest_ms * 1e-3)
+
+
 class Clocks:
     """nvidia-smi clock/throttle sampling while the timed region runs."""
 
@@ -203,12 +219,8 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def slowest(x):
+        return max_over_ranks(dist, x, "cuda")
 
     def timed(flux, chem, steps, warmup, timing=False, clocks=None, resident=False):
         st = hf.Stepper(ctx, level, torch.from_numpy(U0).cuda(), flux=flux, chem=chem)
@@ -239,17 +251,17 @@ def run_ours(args):
             ctx.set_timing(False)
         c1 = ctx.counters()
         st.close()
-        return max_over_ranks(ms), ck, tm, {k: c1[k] - c0[k] for k in c1}
+        return slowest(ms), ck, tm, {k: c1[k] - c0[k] for k in c1}
 
     clocks = Clocks(local)
     ms, ck, tm, cnt = timed(args.flux, args.chem, args.steps, args.warmup, timing=True, clocks=clocks,
                             resident=args.chem == "persistent")
-    value = world * cells * args.steps / (ms * 1e-3)
+    value = replica_value(world, cells, args.steps, ms)
     plain = None
     if not args.no_plain:
         ps = args.plain_steps or args.steps
         pms, _, ptm, pcnt = timed("plain", "plain", ps, args.warmup, timing=True)
-        plain = {"value": world * cells * ps / (pms * 1e-3), "ms_per_step": pms / ps, "steps": ps,
+        plain = {"value": replica_value(world, cells, ps, pms), "ms_per_step": pms / ps, "steps": ps,
                  "chem_ms_per_step": ptm["chem"][0] / ps, "flux_ms_per_step": ptm["flux"][0] / ps}
 
     chem_batch = None
@@ -269,8 +281,8 @@ def run_ours(args):
             cb.advance(field, 0.0, dt_cell=dtc)
             e1.record()
             barrier()
-            cms = max_over_ranks(e0.elapsed_time(e1))
-            chem_batch[form] = {"ms": cms, "cells_per_s": world * args.chem_cells / (cms * 1e-3)}
+            cms = slowest(e0.elapsed_time(e1))
+            chem_batch[form] = {"ms": cms, "cells_per_s": replica_value(world, args.chem_cells, 1, cms)}
             del field
         chem_batch["batched_over_plain"] = chem_batch["plain"]["ms"] / chem_batch["batched"]["ms"]
 
@@ -296,7 +308,7 @@ def run_ours(args):
             Ja, Ga, _ = sa.adjoint(Ua)
             e2.record()
             barrier()
-            fms, ams = max_over_ranks(e0.elapsed_time(e1)), max_over_ranks(e1.elapsed_time(e2))
+            fms, ams = slowest(e0.elapsed_time(e1)), slowest(e1.elapsed_time(e2))
             ok = ~torch.isnan(Jf)
             adjoint[obj] = {"forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
                             "cells_with_objective": int(ok.sum().item()),
@@ -330,8 +342,8 @@ def run_ours(args):
         ea.record()
         barrier()
         t3 = time.perf_counter()
-        fwd = max_over_ranks(e0.elapsed_time(e1))
-        adj = max_over_ranks(e2.elapsed_time(ea))
+        fwd = slowest(e0.elapsed_time(e1))
+        adj = slowest(e2.elapsed_time(ea))
         fa.close()
         if adjoint is None:
             adjoint = {}
@@ -421,10 +433,10 @@ def run_ours(args):
             st.step(cfl=args.cfl)
             st.get_host(host)
         barrier()
-        el = max_over_ranks(time.perf_counter() - t0)
+        el = slowest(time.perf_counter() - t0)
         st.close()
         nbytes = nv * cells * 8
-        e2e = {"value": world * cells * args.steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": nbytes,
+        e2e = {"value": replica_value(world, cells, args.steps, el * 1e3), "unit": "cell-steps/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes}
 
     if rank != 0:
