@@ -435,7 +435,7 @@ static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const 
                              double dt, const double* dt_cell, double rtol, double atol, int form,
                              const hf_chem_history* hist, int64_t* first_failed, void* stream) {
     if (first_failed) *first_failed = -1;
-    if (!ctx || !U || count < 0 || count > INT32_MAX || (!cell_index && comp_stride < count) ||
+    if (!ctx || (!U && count > 0) || count < 0 || count > INT32_MAX || (!cell_index && comp_stride < count) ||
         (!dt_cell && (!(dt > 0) || !std::isfinite(dt))) || !(rtol > 0) || !(atol > 0) ||
         (form != HF_CHEM_PLAIN && form != HF_CHEM_PERSISTENT && form != 2))
         return fail(ctx, HF_ERR_ARG, "chem_advance: invalid batch extent, interval or tolerances");

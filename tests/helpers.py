@@ -85,3 +85,14 @@ def comp_err(a, b):
     a2, b2 = a.reshape(-1, nv), b.reshape(-1, nv)
     scale = np.maximum(np.max(np.abs(b2), axis=0), 1e-300)
     return float(np.max(np.abs(a2 - b2) / scale))
+
+
+def ghosted_field(nx, ny, seed=0, ns=9):
+    """(ny+4, nx+4, NV) smooth field with periodic ghost layers (no oracle needed)."""
+    return np.pad(smooth_field(nx, ny, seed=seed, ns=ns), ((2, 2), (2, 2), (0, 0)), mode="wrap")
+
+
+def chem_cells(n, seed=0):
+    """(NV, n) independent 0D cells of uneven stiffness, N2 diluent (9 species)."""
+    from hyperflow_gb300 import workloads as W
+    return W.chem_batch(n, seed=seed, diluent="N2")[0]
