@@ -174,6 +174,40 @@ def cpu_sample(steps=2, warm=1, rows=4, threads=0, nx=NX, flux_threads=0):
             "seconds": el}
 
 
+def tight_errors(states, ref_states):
+    """T relative and Y_k absolute errors (max over cells) of AoS states against the
+    tight oracle's; Y_k = rho Y_k / rho of the reference."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.set_species(10)
+    Tg, Tr = oracle.properties(states)[2], oracle.properties(ref_states)[2]
+    rho = ref_states[:, :10].sum(1)
+    return {"T_rel_max": float(np.max(np.abs(Tg - Tr) / Tr)),
+            "Y_abs_max": float(np.max(np.abs(states[:, :10] - ref_states[:, :10]) / rho[:, None]))}
+
+
+def tight_oracle_strip(U0, lvd, dts, nx, rows):
+    """The oracle's Strang steps of a strip at rtol 1e-12 / atol 1e-20 with the given
+    step sizes (AoS interior states)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    oracle.set_species(10)
+    oracle.set_flux_threads(0)
+    g = oracle.make_grid(nx, rows, lvd["dx"], lvd["dy"], periodic=(0, 1), bc_lo=(0, 0), bc_hi=(1, 0),
+                         inlet=lvd["inlet"])
+    Ug = oracle.ghosted(U0.transpose(1, 2, 0))
+    try:
+        for dt in dts:
+            Ug, dta, st, _ = oracle.strang_step(g, Ug, dt, rtol=1e-12, atol=1e-20)
+            if st or dta != dt:
+                raise RuntimeError("tight oracle step failed")
+    finally:
+        oracle.set_flux_threads(1)
+    return Ug[2:-2, 2:-2].reshape(-1, U0.shape[0])
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -265,6 +299,7 @@ def run_ours(args):
                  "chem_ms_per_step": ptm["chem"][0] / ps, "flux_ms_per_step": ptm["flux"][0] / ps}
 
     chem_batch = None
+    chem_sample = None
     if args.chem_cells > 0:
         # chemistry-only batch of independent 0D cells with very uneven stiffness
         # (T ~ U[800,2500] K, p ~ logU[0.1,10] atm, phi ~ logU[0.3,3], Ar ~ U[0,0.8],
@@ -283,6 +318,8 @@ def run_ours(args):
             barrier()
             cms = slowest(e0.elapsed_time(e1))
             chem_batch[form] = {"ms": cms, "cells_per_s": replica_value(world, args.chem_cells, 1, cms)}
+            if form == "batched":  # a sample for the error against the tight oracle
+                chem_sample = (field[:, :512].cpu().numpy().T.copy(), Uc[:, :512].T.copy(), dtc_np[:512].copy())
             del field
         chem_batch["batched_over_plain"] = chem_batch["plain"]["ms"] / chem_batch["batched"]["ms"]
 
@@ -461,6 +498,37 @@ def run_ours(args):
                      "flops_per_attempt": FLOPS_PER_ATTEMPT},
             "note": "the chemistry kernel is FP64-pipe bound, not HBM bound: the HBM fraction is reported per "
                     "the contract, the fp64 object is the binding roof; traffic = ncu dram bytes per launch"}
+    accuracy = None
+    if not args.no_cpu and rank == 0:
+        # error of this build's results against the tight FP64 oracle (rtol 1e-12,
+        # atol 1e-20): 2 graph steps of a 2048 x 4 strip of the same detonation (the
+        # oracle replays the GPU's step sizes), and 512 cells of the uneven chemistry batch
+        rows = 4
+        Us, ls = W.det2d(seed=0, diluent="AR", nx=args.nx, ny=rows)
+        ss = hf.Stepper(ctx, hf.make_level(**ls), torch.from_numpy(Us).cuda(), flux=args.flux, chem=args.chem)
+        dts = [ss.step(cfl=args.cfl) for _ in range(2)]
+        got = ss.state().cpu().numpy().transpose(1, 2, 0).reshape(-1, nv)
+        ss.close()
+        t0 = time.perf_counter()
+        ref = tight_oracle_strip(Us, ls, dts, args.nx, rows)
+        accuracy = {"oracle": "CPU restatement, Rodas4 at rtol 1e-12 / atol 1e-20", "target": "T rel <= 1e-6",
+                    "strip": dict(tight_errors(got, ref), cells=args.nx * rows, steps=2,
+                                  oracle_seconds=time.perf_counter() - t0)}
+        if chem_sample is not None:
+            # per cell with a step limit the tight tolerance needs (the 5000-step limit
+            # of the reference's integrator is for its own rtol 1e-8)
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.set_species(10)
+            gotc, U0c, dtc_s = chem_sample
+            refc = np.empty_like(U0c)
+            ok = True
+            for k in range(len(U0c)):
+                refc[k], stc, _ = oracle.chem_advance(U0c[k], dtc_s[k], rtol=1e-12, atol=1e-20, max_steps=10 ** 6)
+                ok = ok and stc == 0
+            if ok:
+                accuracy["chem_batch"] = dict(tight_errors(gotc, refc), cells=len(U0c))
+
     cpu = None
     if not args.no_cpu:
         # all host threads on every loop (the baseline), and the reference's threading
@@ -486,7 +554,8 @@ def run_ours(args):
         "chem_attempts_per_cell_step": cnt["chem_steps"] / max(cnt["chem_cell_calls"], 1),
         "plain": plain, "batched_over_plain": (value / plain["value"]) if plain else None,
         "chem_batch_uneven": chem_batch,
-        "roofline": roof, "cpu_baseline": cpu, "adjoint": adjoint, "det1d": det1d, "amr": amr,
+        "roofline": roof, "cpu_baseline": cpu, "accuracy": accuracy, "adjoint": adjoint, "det1d": det1d,
+        "amr": amr,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
