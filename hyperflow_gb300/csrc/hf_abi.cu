@@ -603,13 +603,29 @@ hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch* patches,
                     double* dt, void* stream) {
     if (!ctx || !level || !patches || npatch <= 0 || !U || !dt || !(cfl > 0) || !level_ok(*level))
         return fail(ctx, HF_ERR_ARG, "cfl_dt: bad arguments");
+    for (int p = 0; p < npatch; ++p)
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "cfl_dt: bad patch");
     const cudaStream_t s = S(stream);
     const Level L = make_level(*level);
+    std::vector<int64_t> base;
+    if (npatch > 1) {  // every patch in one launch
+        base.resize(npatch);
+        int64_t b = 0;
+        for (int p = 0; p < npatch; ++p) {
+            base[p] = b;
+            b += (int64_t)patches[p].nx * patches[p].ny;
+        }
+        HF_CUDA(upload_patches(ctx, patches, npatch, s));
+        HF_CUDA(upload_offsets(ctx, base.data(), npatch, s));
+    }
     HF_CUDA(reset_status(ctx, s));
     tic(ctx, 2, s);
-    for (int p = 0; p < npatch; ++p)
-        HF_CUDA(launch_cfl(ctx->ns, L, patches[p], U, ctx->st, s, &ctx->cnt.kernel_launches));
-    toc(ctx, s, npatch);
+    if (npatch == 1)
+        HF_CUDA(launch_cfl(ctx->ns, L, patches[0], U, ctx->st, s, &ctx->cnt.kernel_launches));
+    else
+        HF_CUDA(launch_cfl_multi(ctx->ns, L, patches, ctx->d_patches, npatch, ctx->d_off, U, ctx->st, s,
+                                 &ctx->cnt.kernel_launches));
+    toc(ctx, s, 1);
     HF_CUDA(read_status(ctx, s));
     if (ctx->st_host->flags) return fail(ctx, HF_ERR_INADMISSIBLE, "cfl_dt: inadmissible cell");
     double rate;
@@ -622,15 +638,27 @@ hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patche
                       int64_t* bad_cell, void* stream) {
     if (bad_cell) *bad_cell = -1;
     if (!ctx || !level || !patches || npatch <= 0 || !U) return fail(ctx, HF_ERR_ARG, "validate: bad arguments");
+    for (int p = 0; p < npatch; ++p)
+        if (!patch_ok(patches[p])) return fail(ctx, HF_ERR_ARG, "validate: bad patch");
     const cudaStream_t s = S(stream);
+    std::vector<int64_t> base(npatch);
+    int64_t b = 0;
+    for (int p = 0; p < npatch; ++p) {
+        base[p] = b;
+        b += (int64_t)patches[p].nx * patches[p].ny;
+    }
+    if (npatch > 1) {  // every patch in one launch
+        HF_CUDA(upload_patches(ctx, patches, npatch, s));
+        HF_CUDA(upload_offsets(ctx, base.data(), npatch, s));
+    }
     HF_CUDA(reset_status(ctx, s));
     tic(ctx, 2, s);
-    int64_t base = 0;
-    for (int p = 0; p < npatch; ++p) {
-        HF_CUDA(launch_validate(ctx->ns, patches[p], U, base, ctx->st, s, &ctx->cnt.kernel_launches));
-        base += (int64_t)patches[p].nx * patches[p].ny;
-    }
-    toc(ctx, s, npatch);
+    if (npatch == 1)
+        HF_CUDA(launch_validate(ctx->ns, patches[0], U, 0, ctx->st, s, &ctx->cnt.kernel_launches));
+    else
+        HF_CUDA(launch_validate_multi(ctx->ns, patches, ctx->d_patches, npatch, ctx->d_off, U, ctx->st, s,
+                                      &ctx->cnt.kernel_launches));
+    toc(ctx, s, 1);
     HF_CUDA(read_status(ctx, s));
     if (ctx->st_host->flags) {
         if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;

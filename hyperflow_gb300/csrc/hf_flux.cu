@@ -659,9 +659,8 @@ __global__ void k_combine(hf_patch P, const double* __restrict__ Uold, double* _
     if (!properties<NS>(q, p, 1000.0)) flag(st, ST_COMBINE_BAD, cell_base + idx);
 }
 template <int NS>
-__global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cell_base, DevStatus* st) {
-    if (st->abort_run) return;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void validate_one(const hf_patch& P, const double* __restrict__ U, int64_t cell_base,
+                                             DevStatus* st, int64_t idx) {
     if (idx >= (int64_t)P.nx * P.ny) return;
     const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
     const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
@@ -672,9 +671,23 @@ __global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cel
     if (!properties<NS>(q, p, 1000.0)) flag(st, ST_STAGE_BAD, cell_base + idx);
 }
 template <int NS>
-__global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStatus* st) {
+__global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cell_base, DevStatus* st) {
     if (st->abort_run) return;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    validate_one<NS>(P, U, cell_base, st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+// every patch of a level in one launch: patch blockIdx.y, its first cell index base[p]
+template <int NS>
+__global__ void k_validate_multi(const hf_patch* __restrict__ patches, const int64_t* __restrict__ base,
+                                 const double* __restrict__ U, DevStatus* st) {
+    const hf_patch P = patches[blockIdx.y];
+    validate_one<NS>(P, U, base[blockIdx.y], st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// CFL rate of cell idx of patch P (0 outside it or when inadmissible, which is flagged
+// with bad index cell_base + idx); the block's warps fold it into st->rate_bits.
+template <int NS>
+__device__ __forceinline__ void cfl_one(const Level& L, const hf_patch& P, const double* __restrict__ U,
+                                        int64_t cell_base, DevStatus* st, int64_t idx) {
     double rate = 0.0;
     if (idx < (int64_t)P.nx * P.ny) {
         const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
@@ -684,7 +697,7 @@ __global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStat
         for (int n = 0; n < NS + 3; ++n) q[n] = U[g + n * P.comp_stride];
         Props p;
         if (!properties<NS>(q, p, 1000.0)) {
-            flag(st, ST_STAGE_BAD, idx);
+            flag(st, ST_STAGE_BAD, cell_base + idx);
         } else {
             double rho = 0.0;
 #pragma unroll
@@ -695,6 +708,17 @@ __global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStat
     // warp max then one atomic per warp (max is order independent: deterministic)
     for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
     if ((threadIdx.x & 31) == 0 && rate > 0.0) atomicMax(&st->rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+template <int NS>
+__global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStatus* st) {
+    if (st->abort_run) return;
+    cfl_one<NS>(L, P, U, 0, st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <int NS>
+__global__ void k_cfl_multi(Level L, const hf_patch* __restrict__ patches, const int64_t* __restrict__ base,
+                            const double* __restrict__ U, DevStatus* st) {
+    const hf_patch P = patches[blockIdx.y];
+    cfl_one<NS>(L, P, U, base[blockIdx.y], st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 #define HF_DISPATCH(ns, call) ((ns) == 9 ? call<9> : call<10>)
@@ -709,6 +733,25 @@ cudaError_t launch_validate(int ns, const hf_patch& P, const double* U, int64_t 
                             cudaStream_t s, int64_t* launches) {
     const int64_t n = (int64_t)P.nx * P.ny;
     HF_DISPATCH(ns, k_validate)<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, U, cell_base, st);
+    ++*launches;
+    return cudaGetLastError();
+}
+cudaError_t launch_validate_multi(int ns, const hf_patch* ph, const hf_patch* pd, int npatch, const int64_t* base_dev,
+                                  const double* U, DevStatus* st, cudaStream_t s, int64_t* launches) {
+    int64_t mc = 1;
+    for (int p = 0; p < npatch; ++p) mc = max(mc, (int64_t)ph[p].nx * ph[p].ny);
+    HF_DISPATCH(ns, k_validate_multi)<<<dim3((unsigned)((mc + 127) / 128), (unsigned)npatch), 128, 0, s>>>(
+        pd, base_dev, U, st);
+    ++*launches;
+    return cudaGetLastError();
+}
+cudaError_t launch_cfl_multi(int ns, const Level& L, const hf_patch* ph, const hf_patch* pd, int npatch,
+                             const int64_t* base_dev, const double* U, DevStatus* st, cudaStream_t s,
+                             int64_t* launches) {
+    int64_t mc = 1;
+    for (int p = 0; p < npatch; ++p) mc = max(mc, (int64_t)ph[p].nx * ph[p].ny);
+    HF_DISPATCH(ns, k_cfl_multi)<<<dim3((unsigned)((mc + 127) / 128), (unsigned)npatch), 128, 0, s>>>(L, pd, base_dev,
+                                                                                                     U, st);
     ++*launches;
     return cudaGetLastError();
 }

@@ -82,6 +82,13 @@ cudaError_t launch_dt_from_rate(const DevStatus* st, double cfl, double* dt, cud
 bool make_tensor_map(void* tmap, const double* base, const hf_patch& P, int nv);
 cudaError_t launch_combine(int ns, const hf_patch& P, const double* Uold, double* U, int64_t cell_base,
                            DevStatus* st, cudaStream_t s, int64_t* launches);
+// Every patch of a level in one launch; base_dev[p] = patch p's first cell index.
+cudaError_t launch_validate_multi(int ns, const hf_patch* patches_host, const hf_patch* patches_dev, int npatch,
+                                  const int64_t* base_dev, const double* U, DevStatus* st, cudaStream_t s,
+                                  int64_t* launches);
+cudaError_t launch_cfl_multi(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
+                             int npatch, const int64_t* base_dev, const double* U, DevStatus* st, cudaStream_t s,
+                             int64_t* launches);
 cudaError_t launch_validate(int ns, const hf_patch& P, const double* U, int64_t cell_base, DevStatus* st,
                             cudaStream_t s, int64_t* launches);
 cudaError_t launch_cfl(int ns, const Level& L, const hf_patch& P, const double* U, DevStatus* st,

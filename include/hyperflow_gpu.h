@@ -171,7 +171,9 @@ HF_EXPORT hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_
  * index of cell i's component 0, components comp_stride apart).  dt: one interval for all,
  * or dt_cell[i] per cell when dt_cell is non-NULL (extension).  rtol/atol: 1e-8/1e-15 in
  * the reference.  All-or-nothing: on failure U is unchanged and *first_failed is the lowest
- * failing cell index.  form: HF_CHEM_PLAIN or HF_CHEM_PERSISTENT. ---- */
+ * failing cell index.  form: HF_CHEM_PLAIN or HF_CHEM_PERSISTENT.  count 0 is a no-op
+ * (U may then be NULL); a negative count, count > comp_stride without cell_index, dt <= 0
+ * without dt_cell, or non-positive tolerances return HF_ERR_ARG before any device work. ---- */
 HF_EXPORT hf_status hf_chem_advance(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index,
                           int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                           int form, int64_t* first_failed, void* stream);
