@@ -99,3 +99,53 @@ def test_tagging_matches_oracle(gpu, oracle):
     got = hf.tag_cells(gpu, lv, ps, 1e-7, pressure_tag=0.08, temperature_tag=0.06, fuel_rate_tag=50.0,
                        density_tag=0.05, chemistry=True, box=(0.0005, 0.001, 0.0, 0.0008), velocity=(300.0, 0.0))
     assert np.array_equal(got.cpu().numpy().reshape(ny, nx), ref)
+
+
+def test_multi_patch_launches_equal_single_patch(gpu):
+    """One launch over every patch of a level (the multi-patch face/update, validation and
+    CFL kernels) gives the bits of one call per patch."""
+    import ctypes
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import _lib as L
+    lib, hh = gpu.lib, gpu.h
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    nx, ny, nv = 48, 24, 12
+    boxes = [(0, 0, 15, 11), (16, 0, 47, 11), (0, 12, 31, 23), (32, 12, 47, 23)]  # the whole domain
+    lv = hf.make_level(nx, ny, 1e-4, 1e-4, periodic=(1, 1))
+    field = H.smooth_field(nx, ny, seed=9)
+    src = hf.PatchSet(nv, boxes)
+    for k, (i0, j0, i1, j1) in enumerate(boxes):
+        src.interior(k).copy_(cuda(field[j0:j1 + 1, i0:i1 + 1].transpose(2, 0, 1)))
+    gpu.check(lib.hf_fill_ghosts(hh, ctypes.byref(lv), src.patches, len(boxes), p(src.data), s), "fill")
+    dt = ctypes.c_double()
+    gpu.check(lib.hf_cfl_dt(hh, ctypes.byref(lv), src.patches, len(boxes), p(src.data), 0.5, ctypes.byref(dt), s),
+              "cfl")
+    one = []
+    for k in range(len(boxes)):
+        d = ctypes.c_double()
+        gpu.check(lib.hf_cfl_dt(hh, ctypes.byref(lv), ctypes.byref(src.patches[k]), 1, p(src.data), 0.5,
+                                ctypes.byref(d), s), "cfl")
+        one.append(d.value)
+    assert dt.value == min(one)
+    bad = ctypes.c_int64()
+    out_all = hf.PatchSet(nv, boxes)
+    out_one = hf.PatchSet(nv, boxes)
+    gpu.check(lib.hf_flux_update(hh, ctypes.byref(lv), src.patches, len(boxes), p(src.data), None, p(out_all.data),
+                                 None, None, 0.5 * dt.value, 0, L.HF_FLUX_PLAIN, ctypes.byref(bad), s), "flux")
+    for k in range(len(boxes)):
+        gpu.check(lib.hf_flux_update(hh, ctypes.byref(lv), ctypes.byref(src.patches[k]), 1, p(src.data), None,
+                                     p(out_one.data), None, None, 0.5 * dt.value, 0, L.HF_FLUX_PLAIN,
+                                     ctypes.byref(bad), s), "flux")
+    assert torch.equal(out_all.data, out_one.data)
+    assert not torch.equal(out_all.interior(0), src.interior(0))
+    # validation: the bad cell's index counts the cells of the patches before it
+    out_all.interior(2)[0, 5, 7] = -1.0
+    b_all, b_one = ctypes.c_int64(-1), ctypes.c_int64(-1)
+    assert lib.hf_validate(hh, ctypes.byref(lv), out_all.patches, len(boxes), p(out_all.data), ctypes.byref(b_all),
+                           s) == L.HF_ERR_INADMISSIBLE
+    assert lib.hf_validate(hh, ctypes.byref(lv), ctypes.byref(out_all.patches[2]), 1, p(out_all.data),
+                           ctypes.byref(b_one), s) == L.HF_ERR_INADMISSIBLE
+    before = sum(out_all.patches[k].nx * out_all.patches[k].ny for k in range(2))
+    assert b_one.value == 5 * out_all.patches[2].nx + 7
+    assert b_all.value == before + b_one.value
