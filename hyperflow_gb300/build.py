@@ -13,6 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhyperflow_gpu.so")
+HOST_SRC = os.path.join(HERE, "host", "hf_host_run.c")
+HOST_BIN = os.path.join(HERE, "hf_host_run")  # C host over the ABI (gcc; no CUDA headers)
 SOURCES = ["hf_flux.cu", "hf_chem.cu", "hf_amr.cu", "hf_abi.cu", "hf_stepper.cu", "hf_adjoint.cu",
            "hf_flux_adjoint.cu", "hf_flow_adjoint.cu", "hf_amr_stepper.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -64,6 +66,16 @@ def build(verbose=False, ptxas_info=False):
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    if not os.path.exists(HOST_BIN) or os.path.getmtime(HOST_BIN) < max(os.path.getmtime(HOST_SRC),
+                                                                          os.path.getmtime(LIB)):
+        cmd = [os.environ.get("CC", "gcc"), "-std=c99", "-O2", "-Wall", "-Wextra", "-I",
+               os.path.join(HERE, "..", "include"), HOST_SRC, "-o", HOST_BIN, "-L", HERE, "-lhyperflow_gpu",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode or r.stderr:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError("host program build failed")
     return LIB
 
 

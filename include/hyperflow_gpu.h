@@ -381,7 +381,8 @@ HF_EXPORT hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_pat
  * BlockAMR.cpp:409-419): Strang flow(dt/2), react(dt), flow(dt/2), each flow a Heun pair
  * of Euler stages; rollback and dt halving up to 18 attempts. ---- */
 typedef struct hf_stepper hf_stepper;
-/* U0: initial valid cells, SoA [NV][ny][nx] in DEVICE memory (copied in). */
+/* U0: initial valid cells, SoA [NV][ny][nx] in DEVICE memory (copied in); NULL starts
+ * from zeros, for a host that loads the state with hf_stepper_set_host. */
 HF_EXPORT hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0, int chemistry,
                             double rtol, double atol, int flux_form, int chem_form,
                             hf_stepper** out);
