@@ -13,8 +13,8 @@ memory, copied in and out every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-With N > 1 (torchrun) every rank runs an independent replica (the reacting step of
-one grid does not shard across these GPUs in this build): value = all ranks' cell-steps
+With N > 1 (torchrun) every rank runs an independent replica (one grid per GPU; the
+step of one grid is not sharded): value = all ranks' cell-steps
 over the slowest rank's time.  --impl reference times the CPU restatement of the
 reference (the reference itself needs Cantera, SUNDIALS and AMReX, absent here) on
 this host's cores over a bounded sample of the same workload.
@@ -500,7 +500,7 @@ def run_ours(args):
                     "the contract, the fp64 object is the binding roof; traffic = ncu dram bytes per launch"}
     accuracy = None
     if not args.no_cpu and rank == 0:
-        # error of this build's results against the tight FP64 oracle (rtol 1e-12,
+        # error of the GPU results against the tight FP64 oracle (rtol 1e-12,
         # atol 1e-20): 2 graph steps of a 2048 x 4 strip of the same detonation (the
         # oracle replays the GPU's step sizes), and 512 cells of the uneven chemistry batch
         rows = 4

@@ -1,6 +1,6 @@
 // CPU oracle for the HyperFlow V3 reacting-Euler step.  TEST INFRASTRUCTURE ONLY:
-// tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg call it as the
-// checker; the GPU library never links, loads or calls it.
+// tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg call it to check
+// results; the GPU library never links, loads or calls it.
 //
 // It restates, in plain C++17 on the reference's own AoS state layout
 // (12 doubles per cell: rhoY_0..rhoY_8, rho*u, rho*v, rho*E), the semantics of

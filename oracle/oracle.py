@@ -1,7 +1,7 @@
 """ctypes wrapper around the CPU oracle (``liboracle.so``).
 
 Test infrastructure only: the tests, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` use it as the checker.  The GPU package never
+baseline leg of ``bench.py`` use it to check results.  The GPU package never
 imports it.  States are AoS float64 arrays of shape (..., NS+3) in the
 reference's component order (rhoY_0..rhoY_{NS-1}, rho*u, rho*v, rho*E).
 """
