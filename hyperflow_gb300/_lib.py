@@ -92,6 +92,8 @@ SIGNATURES = [
     ("hf_amr_get_level", _i32, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     ("hf_amr_totals", _i32, [_vp, _dp, _vp]),
     ("hf_amr_time", _d, [_vp]),
+    ("hf_amr_set_graph", None, [_vp, ctypes.c_int]),
+    ("hf_amr_stats", None, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     ("hf_flow_record", _i32, [_vp, ctypes.POINTER(Level), _vp, _i32, _vp, _d, _i32, ctypes.c_int, _d, _d, _vp, _vp,
                               ctypes.POINTER(_vp), _vp]),
     ("hf_flow_adjoint", _i32, [_vp, _vp, _vp, _vp, _vp]),

@@ -149,7 +149,8 @@ __global__ void k_reflux(Level L, const hf_patch* __restrict__ coarse, const int
                          const double* __restrict__ fyc, double* __restrict__ Uc, const hf_patch* __restrict__ fine,
                          const int64_t* __restrict__ ffx_off, const int64_t* __restrict__ ffy_off,
                          const double* __restrict__ fxf, const double* __restrict__ fyf,
-                         const int* __restrict__ cover, double h, int nv) {
+                         const int* __restrict__ cover, double h, const double* __restrict__ hdev, int nv) {
+    if (hdev) h = *hdev;  // stage length from device memory (graph-captured steps)
     const hf_patch C = coarse[blockIdx.y];
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)C.nx * C.ny) return;
@@ -207,7 +208,7 @@ cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_p
                           const int64_t* cfx_off, const int64_t* cfy_off, const double* fxc, const double* fyc,
                           double* Uc, const hf_patch* fine_dev, const hf_patch* fine_host, int nfine,
                           const int64_t* ffx_off, const int64_t* ffy_off, const double* fxf, const double* fyf,
-                          int* cover, double h, int nv, cudaStream_t s, int64_t* launches) {
+                          int* cover, double h, int nv, cudaStream_t s, int64_t* launches, const double* hdev) {
     const int64_t nc = (int64_t)L.nx * L.ny;
     k_cover_clear<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(cover, nc);
     int64_t mf = 1;
@@ -216,7 +217,7 @@ cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_p
     int64_t mc = 1;
     for (int p = 0; p < ncoarse; ++p) mc = max(mc, (int64_t)coarse_host[p].nx * coarse_host[p].ny);
     k_reflux<<<dim3((unsigned)((mc + 127) / 128), (unsigned)ncoarse), 128, 0, s>>>(
-        L, coarse_dev, cfx_off, cfy_off, fxc, fyc, Uc, fine_dev, ffx_off, ffy_off, fxf, fyf, cover, h, nv);
+        L, coarse_dev, cfx_off, cfy_off, fxc, fyc, Uc, fine_dev, ffx_off, ffy_off, fxf, fyf, cover, h, hdev, nv);
     *launches += 3;
     return cudaGetLastError();
 }

@@ -47,6 +47,18 @@ struct AmrLevel {
     int32_t* d_regions = nullptr;   // coarse-fine ghost regions (4 int32 each, device)
     int nregions = 0;
     int64_t region_cells = 1;       // largest coarsened region
+    // device tables of the graph-captured step (uploaded at rebuild; capacity: every block)
+    hf_patch* d_patches = nullptr;
+    int64_t* d_foff = nullptr;      // 3 per patch: x-face offset, y-face offset, first cell
+    int64_t* d_xoff = nullptr;      // x-face offset per patch (reflux)
+    int64_t* d_yoff = nullptr;      // y-face offset per patch (reflux)
+    int64_t* d_base = nullptr;      // first cell per patch (validation, CFL)
+    int* cover = nullptr;           // reflux cover map over the level's cells
+    // batched chemistry scratch of the graph-captured step (allocated on first capture)
+    double* trial = nullptr;
+    int* fail = nullptr;
+    int32_t* order = nullptr;
+    unsigned long long* bins = nullptr;
     size_t bytes = 0;
     double *U = nullptr, *S = nullptr, *N = nullptr, *O = nullptr, *B = nullptr;  // state, stage, next, old, backup
     double *fx = nullptr, *fy = nullptr;  // face fluxes packed per patch (capacity: every block)
@@ -71,6 +83,19 @@ struct hf_amr {
     int finest = 0;
     double time = 0.0;
     int64_t steps = 0, regrids = 0;
+    // graph-captured steps: state in U, result in O.  A graph captures the buffer
+    // pointers of the moment (the host path swaps U and N, the graph path U and O), so
+    // each of the two graphs is keyed by level 0's pointers; both are dropped at regrid
+    hf::DevStatus* gst = nullptr;
+    hf::DevStatus* gst_host = nullptr;
+    double* ddt = nullptr;       // device [dt, dt/2]
+    double* ddt_host = nullptr;
+    double* key[2][4] = {};      // level 0's U, N, S, O when graph k was captured
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int64_t graph_kernels[2] = {0, 0};
+    double graph_cfl = -1.0;
+    int use_graph = 1, sm_count = 1;
+    int64_t graph_steps = 0, host_steps = 0;
 };
 
 namespace {
@@ -131,6 +156,36 @@ hf_status rebuild(hf_amr* m, cudaStream_t s) {
             cudaMemsetAsync(a.hist.cost, 0, sizeof(int32_t) * std::max<int64_t>(a.nleaf, 1), s) != cudaSuccess)
             return HF_ERR_CUDA;
     }
+    // device tables of the graph-captured step (face arrays packed per patch as
+    // hf_flux_update packs them); the graphs captured for the old blocks are stale
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        const int np = (int)a.patches.size();
+        std::vector<int64_t> foff(3 * (size_t)np), xo(np), yo(np), base(np);
+        int64_t ox = 0, oy = 0, b = 0;
+        for (int p = 0; p < np; ++p) {
+            const hf_patch& P = a.patches[p];
+            foff[3 * p] = xo[p] = ox;
+            foff[3 * p + 1] = yo[p] = oy;
+            foff[3 * p + 2] = base[p] = b;
+            ox += (int64_t)m->nv * (P.nx + 1) * P.ny;
+            oy += (int64_t)m->nv * P.nx * (P.ny + 1);
+            b += (int64_t)P.nx * P.ny;
+        }
+        if (np && (cudaMemcpyAsync(a.d_patches, a.patches.data(), sizeof(hf_patch) * np, cudaMemcpyHostToDevice, s) !=
+                       cudaSuccess ||
+                   cudaMemcpyAsync(a.d_foff, foff.data(), sizeof(int64_t) * foff.size(), cudaMemcpyHostToDevice, s) !=
+                       cudaSuccess ||
+                   cudaMemcpyAsync(a.d_xoff, xo.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                   cudaMemcpyAsync(a.d_yoff, yo.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                   cudaMemcpyAsync(a.d_base, base.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s) != cudaSuccess))
+            return HF_ERR_CUDA;
+    }
+    for (auto& g : m->exec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     return cuda_st(cudaStreamSynchronize(s));
 }
 
@@ -326,6 +381,198 @@ hf_status totals(hf_amr* m, double* out, cudaStream_t s, int absolute = 0) {
     return HF_OK;
 }
 
+// ---------------------------------------------------------------- graph-captured step
+// The whole Strang step of every level as one CUDA graph: the same kernels as the
+// host-driven path above (multi-patch flux, validation and CFL launches, batched
+// coarse-fine interpolation, reflux and average_down, batched leaf chemistry) with dt
+// computed on the device, every failure a flag in one status block.  The state U of
+// each level is only read; the result goes to O, and the host swaps U and O after a
+// step without flags.  A flagged step is re-run from the untouched U by the host path
+// (first-order redo, repair, rollback and dt halving).
+
+// Ghosts of every level of X (fill_all).
+cudaError_t g_fill_all(hf_amr* m, double* const* X, cudaStream_t s, int64_t* nl) {
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        const hf::Level L = hf::make_level(a.L);
+        cudaError_t e = hf::launch_fill(m->ns, L, a.patches.data(), a.d_patches, (int)a.patches.size(), X[l], s, nl);
+        if (e == cudaSuccess && l > 0)
+            e = hf::launch_interp_regions(m->ns, m->lev[l - 1].dom, X[l - 1], a.dom, X[l], a.d_regions, a.nregions,
+                                          a.region_cells, s, nl);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// average_down of X, finest to coarsest.
+cudaError_t g_average_all(hf_amr* m, double* const* X, cudaStream_t s, int64_t* nl) {
+    for (int l = m->finest; l > 0; --l) {
+        AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
+        cudaError_t e = hf::launch_average_down(f.d_patches, f.patches.data(), (int)f.patches.size(), X[l],
+                                                c.d_patches, (int)c.patches.size(), X[l - 1], m->nv, s, nl);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t g_validate_all(hf_amr* m, double* const* X, cudaStream_t s, int64_t* nl) {
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        cudaError_t e = hf::launch_validate_multi(m->ns, a.patches.data(), a.d_patches, (int)a.patches.size(),
+                                                  a.d_base, X[l], m->gst, s, nl);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// One composite Euler stage in -> out with h from device memory (euler()).
+cudaError_t g_euler(hf_amr* m, double* const* in, double* const* out, const double* hdev, cudaStream_t s, int64_t* nl) {
+    cudaError_t e = g_fill_all(m, in, s, nl);
+    for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        e = hf::launch_flux_multi(m->ns, hf::make_level(a.L), a.patches.data(), a.d_patches, (int)a.patches.size(),
+                                  a.d_foff, in[l], nullptr, out[l], a.fx, a.fy, 0.0, 0, m->gst, s, nl, hdev);
+    }
+    for (int l = m->finest; e == cudaSuccess && l > 0; --l) {
+        AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
+        e = hf::launch_reflux(hf::make_level(c.L), c.d_patches, c.patches.data(), (int)c.patches.size(), c.d_xoff,
+                              c.d_yoff, c.fx, c.fy, out[l - 1], f.d_patches, f.patches.data(), (int)f.patches.size(),
+                              f.d_xoff, f.d_yoff, f.fx, f.fy, c.cover, 0.0, m->nv, s, nl, hdev);
+        if (e == cudaSuccess)
+            e = hf::launch_average_down(f.d_patches, f.patches.data(), (int)f.patches.size(), out[l], c.d_patches,
+                                        (int)c.patches.size(), out[l - 1], m->nv, s, nl);
+    }
+    return e;
+}
+
+// flow(dt/2) in -> out (S stage buffers): two stages, Heun combination, average_down,
+// validation.
+cudaError_t g_flow(hf_amr* m, double* const* in, double* const* S, double* const* out, cudaStream_t s, int64_t* nl) {
+    const double* half = m->ddt + 1;
+    cudaError_t e = g_euler(m, in, S, half, s, nl);
+    if (e == cudaSuccess) e = g_euler(m, S, out, half, s, nl);
+    for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
+        const int64_t n = (int64_t)(m->lev[l].bytes / sizeof(double));
+        k_lincomb_all<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 0.5, in[l], 0.5, out[l]);
+        ++*nl;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = g_average_all(m, out, s, nl);
+    if (e == cudaSuccess) e = g_validate_all(m, out, s, nl);
+    return e;
+}
+
+// react(dt) on the leaf cells of every level of X (react()).
+cudaError_t g_react(hf_amr* m, double* const* X, cudaStream_t s, int64_t* nl) {
+    cudaError_t e = cudaSuccess;
+    for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        if (!a.nleaf) continue;
+        e = cudaMemsetAsync(&m->gst->counter, 0, sizeof(unsigned long long), s);  // work-queue head
+        if (e == cudaSuccess)
+            e = hf::launch_chem_batched(m->ns, X[l], a.dom.comp_stride, a.cells, a.nleaf, 0.0, m->ddt, nullptr,
+                                        m->o.rtol, m->o.atol, a.hist.h, a.hist.cost, a.order, a.bins, a.trial, a.fail,
+                                        m->gst, m->sm_count, s, nl);
+        if (e == cudaSuccess) e = hf::launch_chem_commit(m->ns, X[l], a.dom.comp_stride, a.cells, a.nleaf, a.trial, s, nl);
+    }
+    if (e == cudaSuccess) e = g_average_all(m, X, s, nl);
+    if (e == cudaSuccess) e = g_validate_all(m, X, s, nl);
+    return e;
+}
+
+cudaError_t g_enqueue_step(hf_amr* m, double cfl, cudaStream_t s, int64_t* nl) {
+    double *U[8], *S[8], *N[8], *O[8];
+    arrays(m, [](AmrLevel& a) { return a.U; }, U);
+    arrays(m, [](AmrLevel& a) { return a.S; }, S);
+    arrays(m, [](AmrLevel& a) { return a.N; }, N);
+    arrays(m, [](AmrLevel& a) { return a.O; }, O);
+    cudaError_t e = cudaMemsetAsync(m->gst, 0, sizeof(hf::DevStatus), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&m->gst->bad_cell, 0xff, sizeof(unsigned long long), s);
+    // stableDt over every level (the max rate over all levels' cells)
+    for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        e = hf::launch_cfl_multi(m->ns, hf::make_level(a.L), a.patches.data(), a.d_patches, (int)a.patches.size(),
+                                 a.d_base, U[l], m->gst, s, nl);
+    }
+    if (e == cudaSuccess) e = hf::launch_dt_from_rate(m->gst, cfl, m->ddt, s, nl);
+    if (e == cudaSuccess) e = g_flow(m, U, S, N, s, nl);  // flow(dt/2): U -> N
+    if (e == cudaSuccess && m->o.chemistry) e = g_react(m, N, s, nl);
+    if (e == cudaSuccess) e = g_flow(m, N, S, O, s, nl);  // flow(dt/2): N -> O
+    return e;
+}
+
+// Scratch of the graph path (chemistry per level over its whole dense domain).
+hf_status g_alloc(hf_amr* m) {
+    for (int l = 0; l <= m->o.max_level; ++l) {
+        AmrLevel& a = m->lev[l];
+        if (a.trial) continue;
+        const size_t nc = (size_t)a.L.nx * a.L.ny;
+        if (cudaMalloc(&a.trial, sizeof(double) * m->nv * nc) != cudaSuccess ||
+            cudaMalloc(&a.fail, sizeof(int) * nc) != cudaSuccess ||
+            cudaMalloc(&a.order, sizeof(int32_t) * nc) != cudaSuccess ||
+            cudaMalloc(&a.bins, 16 * sizeof(unsigned long long)) != cudaSuccess)
+            return HF_ERR_CUDA;
+    }
+    return HF_OK;
+}
+
+// One graph step: HF_OK with *dt, HF_ERR_INADMISSIBLE with *dt = the graph's dt when the
+// host path must re-run the step, HF_ERR_CUDA when no graph could be made.
+hf_status g_step(hf_amr* m, double cfl, double* dt, cudaStream_t s) {
+    if (m->graph_cfl != cfl)
+        for (auto& g : m->exec)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    m->graph_cfl = cfl;
+    const AmrLevel& a0 = m->lev[0];
+    const double* now[4] = {a0.U, a0.N, a0.S, a0.O};
+    int k = -1;
+    for (int q = 0; q < 2 && k < 0; ++q)
+        if (m->exec[q] && std::equal(now, now + 4, m->key[q])) k = q;
+    if (k < 0) {  // capture into a free slot (or replace slot 0)
+        k = !m->exec[0] ? 0 : (!m->exec[1] ? 1 : 0);
+        if (m->exec[k]) {
+            cudaGraphExecDestroy(m->exec[k]);
+            m->exec[k] = nullptr;
+        }
+    }
+    if (!m->exec[k]) {
+        if (g_alloc(m) != HF_OK) return HF_ERR_CUDA;
+        cudaStream_t cs = nullptr;
+        cudaGraph_t g = nullptr;
+        int64_t nl = 0;
+        cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t q = g_enqueue_step(m, cfl, cs, &nl);
+            e = cudaStreamEndCapture(cs, &g);
+            if (q != cudaSuccess) e = q;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&m->exec[k], g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (cs) cudaStreamDestroy(cs);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            m->exec[k] = nullptr;
+            return HF_ERR_CUDA;
+        }
+        m->graph_kernels[k] = nl;
+        for (int q = 0; q < 4; ++q) m->key[k][q] = const_cast<double*>(now[q]);
+    }
+    if (cudaGraphLaunch(m->exec[k], s) != cudaSuccess ||
+        cudaMemcpyAsync(m->gst_host, m->gst, sizeof(hf::DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(m->ddt_host, m->ddt, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return HF_ERR_CUDA;
+    int64_t leaf = 0;
+    for (int l = 0; l <= m->finest; ++l) leaf += m->lev[l].nleaf;
+    hf::ctx_add_launches(m->ctx, m->graph_kernels[k], m->o.chemistry ? leaf : 0, (int64_t)m->gst_host->steps);
+    *dt = m->ddt_host[0];
+    return m->gst_host->flags ? HF_ERR_INADMISSIBLE : HF_OK;
+}
+
 // New active blocks of level l+1 from the tags of level l.
 hf_status regrid_level(hf_amr* m, int l, cudaStream_t s) {
     AmrLevel& c = m->lev[l];
@@ -466,7 +713,22 @@ hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, con
              cudaMalloc(&a.hist.h, sizeof(double) * nc) == cudaSuccess &&
              cudaMalloc(&a.hist.cost, sizeof(int32_t) * nc) == cudaSuccess &&
              cudaMalloc(&a.d_regions, sizeof(int32_t) * 4 * 8 * (size_t)a.nbx * a.nby) == cudaSuccess;
+        const size_t cap = (size_t)a.nbx * a.nby;
+        ok = ok && cudaMalloc(&a.d_patches, sizeof(hf_patch) * cap) == cudaSuccess &&
+             cudaMalloc(&a.d_foff, sizeof(int64_t) * 3 * cap) == cudaSuccess &&
+             cudaMalloc(&a.d_xoff, sizeof(int64_t) * cap) == cudaSuccess &&
+             cudaMalloc(&a.d_yoff, sizeof(int64_t) * cap) == cudaSuccess &&
+             cudaMalloc(&a.d_base, sizeof(int64_t) * cap) == cudaSuccess &&
+             cudaMalloc(&a.cover, sizeof(int) * (size_t)nc) == cudaSuccess;
     }
+    int dev = 0;
+    ok = ok && cudaGetDevice(&dev) == cudaSuccess &&
+         cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+         cudaMalloc(&m->gst, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMemset(m->gst, 0, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMallocHost(&m->gst_host, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMalloc(&m->ddt, 2 * sizeof(double)) == cudaSuccess &&
+         cudaMallocHost(&m->ddt_host, 2 * sizeof(double)) == cudaSuccess;
     if (ok) {
         AmrLevel& a = m->lev[0];
         const int64_t nc = (int64_t)a.L.nx * a.L.ny;
@@ -496,7 +758,23 @@ void hf_amr_destroy(hf_amr* m) {
         cudaFree(a.hist.h);
         cudaFree(a.hist.cost);
         cudaFree(a.d_regions);
+        cudaFree(a.d_patches);
+        cudaFree(a.d_foff);
+        cudaFree(a.d_xoff);
+        cudaFree(a.d_yoff);
+        cudaFree(a.d_base);
+        cudaFree(a.cover);
+        cudaFree(a.trial);
+        cudaFree(a.fail);
+        cudaFree(a.order);
+        cudaFree(a.bins);
     }
+    for (auto g : m->exec)
+        if (g) cudaGraphExecDestroy(g);
+    cudaFree(m->gst);
+    cudaFreeHost(m->gst_host);
+    cudaFree(m->ddt);
+    cudaFreeHost(m->ddt_host);
     delete m;
 }
 
@@ -504,6 +782,25 @@ hf_status hf_amr_step(hf_amr* m, double cfl, double* dt, void* stream) {
     if (!m || !dt) return HF_ERR_ARG;
     const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     double h = *dt;
+    if (!(h > 0) && m->use_graph && (!m->o.chemistry || m->o.chem_form == HF_CHEM_PERSISTENT)) {
+        double hg = 0.0;
+        const hf_status r = g_step(m, cfl, &hg, s);
+        if (r == HF_OK) {
+            for (int l = 0; l <= m->finest; ++l) std::swap(m->lev[l].U, m->lev[l].O);
+            m->time += hg;
+            *dt = hg;
+            ++m->steps;
+            ++m->graph_steps;
+            if (m->o.regrid_interval > 0 && m->steps % m->o.regrid_interval == 0) return hf_amr_regrid(m, stream);
+            return HF_OK;
+        }
+        if (r == HF_ERR_CUDA) {
+            m->use_graph = 0;  // no graph: the host-driven path from here on
+            cudaGetLastError();
+        } else {
+            h = hg;  // re-run this step with host control from the untouched U
+        }
+    }
     if (!(h > 0)) {
         // stableDt over the leaf cells of every level (:335-346): the finest level's
         // cells bind (the coarse cells under them are their averages)
@@ -527,6 +824,7 @@ hf_status hf_amr_step(hf_amr* m, double cfl, double* dt, void* stream) {
             m->time += h;
             *dt = h;
             ++m->steps;
+            ++m->host_steps;
             if (m->o.regrid_interval > 0 && m->steps % m->o.regrid_interval == 0) return hf_amr_regrid(m, stream);
             return HF_OK;
         }
@@ -575,5 +873,14 @@ hf_status hf_amr_totals(hf_amr* m, double* out, void* stream) {
 }
 
 double hf_amr_time(const hf_amr* m) { return m ? m->time : 0.0; }
+
+void hf_amr_set_graph(hf_amr* m, int enable) {
+    if (m) m->use_graph = enable ? 1 : 0;
+}
+
+void hf_amr_stats(const hf_amr* m, int64_t* graph_steps, int64_t* host_steps) {
+    if (graph_steps) *graph_steps = m ? m->graph_steps : 0;
+    if (host_steps) *host_steps = m ? m->host_steps : 0;
+}
 
 }  // extern "C"

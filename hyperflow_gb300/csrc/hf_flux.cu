@@ -250,6 +250,7 @@ template <int NS, int D>
 __global__ void __launch_bounds__(128) k_face_multi(Level L, const hf_patch* __restrict__ patches,
                                                     const int64_t* __restrict__ off, const double* __restrict__ U,
                                                     double* __restrict__ F, int first_order, DevStatus* st) {
+    if (st->abort_run) return;
     const int p = blockIdx.y;
     const hf_patch P = patches[p];
     face_one<NS, D>(L, P, U, F + off[3 * p + D], first_order, off[3 * p + 2], st,
@@ -323,7 +324,14 @@ __global__ void __launch_bounds__(128) k_update_multi(const hf_patch* __restrict
                                                       const int64_t* __restrict__ off, const double* __restrict__ Uin,
                                                       const double* __restrict__ Uold, double* __restrict__ Uout,
                                                       const double* __restrict__ FX, const double* __restrict__ FY,
-                                                      double cx, double cy, DevStatus* st) {
+                                                      double cx, double cy, const double* __restrict__ hdev,
+                                                      double dx, double dy, DevStatus* st) {
+    if (st->abort_run) return;
+    if (hdev) {  // stage step from device memory (graph-captured steps): h/dx as on the host
+        const double h = *hdev;
+        cx = h / dx;
+        cy = h / dy;
+    }
     const int p = blockIdx.y;
     const hf_patch P = patches[p];
     update_one<NS>(P, Uin, Uold, Uout, FX + off[3 * p], FY + off[3 * p + 1], cx, cy, off[3 * p + 2], st,
@@ -349,7 +357,7 @@ template <int NS>
 static cudaError_t flux_multi_impl(const Level& L, const hf_patch* ph, const hf_patch* pd, int npatch,
                                    const int64_t* offd, const double* Uin, const double* Uold, double* Uout,
                                    double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
-                                   int64_t* launches) {
+                                   int64_t* launches, const double* hdev) {
     const int bs = 128;
     int64_t mfx = 1, mfy = 1, mc = 1;
     for (int p = 0; p < npatch; ++p) {
@@ -362,18 +370,18 @@ static cudaError_t flux_multi_impl(const Level& L, const hf_patch* ph, const hf_
     k_face_multi<NS, 1><<<dim3((unsigned)((mfy + bs - 1) / bs), (unsigned)npatch), bs, 0, s>>>(L, pd, offd, Uin, FY,
                                                                                              first_order, st);
     k_update_multi<NS><<<dim3((unsigned)((mc + bs - 1) / bs), (unsigned)npatch), bs, 0, s>>>(
-        pd, offd, Uin, Uold, Uout, FX, FY, h / L.dx, h / L.dy, st);
+        pd, offd, Uin, Uold, Uout, FX, FY, h / L.dx, h / L.dy, hdev, L.dx, L.dy, st);
     *launches += 3;
     return cudaGetLastError();
 }
 cudaError_t launch_flux_multi(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
                               int npatch, const int64_t* off_dev, const double* Uin, const double* Uold, double* Uout,
                               double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
-                              int64_t* launches) {
+                              int64_t* launches, const double* hdev) {
     return ns == 9 ? flux_multi_impl<9>(L, patches_host, patches_dev, npatch, off_dev, Uin, Uold, Uout, FX, FY, h,
-                                        first_order, st, s, launches)
+                                        first_order, st, s, launches, hdev)
                    : flux_multi_impl<10>(L, patches_host, patches_dev, npatch, off_dev, Uin, Uold, Uout, FX, FY, h,
-                                         first_order, st, s, launches);
+                                         first_order, st, s, launches, hdev);
 }
 cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int, const double* Uin, const double* Uold,
                               double* Uout, double* fx, double* fy, double h, int first_order, int64_t cell_base,
@@ -679,6 +687,7 @@ __global__ void k_validate(hf_patch P, const double* __restrict__ U, int64_t cel
 template <int NS>
 __global__ void k_validate_multi(const hf_patch* __restrict__ patches, const int64_t* __restrict__ base,
                                  const double* __restrict__ U, DevStatus* st) {
+    if (st->abort_run) return;
     const hf_patch P = patches[blockIdx.y];
     validate_one<NS>(P, U, base[blockIdx.y], st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -717,6 +726,7 @@ __global__ void k_cfl(Level L, hf_patch P, const double* __restrict__ U, DevStat
 template <int NS>
 __global__ void k_cfl_multi(Level L, const hf_patch* __restrict__ patches, const int64_t* __restrict__ base,
                             const double* __restrict__ U, DevStatus* st) {
+    if (st->abort_run) return;
     const hf_patch P = patches[blockIdx.y];
     cfl_one<NS>(L, P, U, base[blockIdx.y], st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }

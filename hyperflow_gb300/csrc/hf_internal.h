@@ -73,7 +73,7 @@ cudaError_t launch_flux_plain(int ns, const Level& L, const hf_patch& P, int pid
 cudaError_t launch_flux_multi(int ns, const Level& L, const hf_patch* patches_host, const hf_patch* patches_dev,
                               int npatch, const int64_t* off_dev, const double* Uin, const double* Uold, double* Uout,
                               double* FX, double* FY, double h, int first_order, DevStatus* st, cudaStream_t s,
-                              int64_t* launches);
+                              int64_t* launches, const double* hdev = nullptr);
 // hdev (nullable): read the stage length h from device memory instead of the argument
 cudaError_t launch_flux_fused(int ns, const Level& L, const hf_patch& P, const void* tmap, const double* Uin,
                               const double* Uold, double* Uout, double h, const double* hdev, int first_order,
@@ -174,7 +174,8 @@ cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_p
                           const int64_t* cfx_off, const int64_t* cfy_off, const double* fxc, const double* fyc,
                           double* Uc, const hf_patch* fine_dev, const hf_patch* fine_host, int nfine,
                           const int64_t* ffx_off, const int64_t* ffy_off, const double* fxf, const double* fyf,
-                          int* cover, double h, int nv, cudaStream_t s, int64_t* launches);
+                          int* cover, double h, int nv, cudaStream_t s, int64_t* launches,
+                          const double* hdev = nullptr);
 cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
                                int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
 

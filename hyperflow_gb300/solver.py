@@ -712,3 +712,13 @@ class AmrStepper:
     @property
     def time(self):
         return self.ctx.lib.hf_amr_time(self.h)
+
+    def set_graph(self, enable=True):
+        """Graph-captured steps (default) or the host-driven path only."""
+        self.ctx.lib.hf_amr_set_graph(self.h, int(bool(enable)))
+
+    def stats(self):
+        """{"graph_steps": n, "host_steps": m}."""
+        g, h = ctypes.c_int64(0), ctypes.c_int64(0)
+        self.ctx.lib.hf_amr_stats(self.h, ctypes.byref(g), ctypes.byref(h))
+        return {"graph_steps": g.value, "host_steps": h.value}

@@ -365,6 +365,13 @@ HF_EXPORT hf_status hf_amr_get_level(hf_amr* amr, int lev, double* U, uint8_t* a
 /* Composite totals over the leaf cells of all levels (host, NV doubles). */
 HF_EXPORT hf_status hf_amr_totals(hf_amr* amr, double* out, void* stream);
 HF_EXPORT double hf_amr_time(const hf_amr* amr);
+/* Graph-captured steps (default on; CFL steps with the batched chemistry form): the whole
+ * multi-level Strang step is one CUDA graph (device dt, one status read per step),
+ * recaptured after every regrid; a step whose graph raises a flag is re-run by the
+ * host-driven path from the untouched start state.  Extension: the reference has no
+ * device graph. */
+HF_EXPORT void hf_amr_set_graph(hf_amr* amr, int enable);
+HF_EXPORT void hf_amr_stats(const hf_amr* amr, int64_t* graph_steps, int64_t* host_steps);
 
 
 /* ---- reductions ---- */

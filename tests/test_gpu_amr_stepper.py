@@ -135,3 +135,36 @@ def test_amr_wedge_three_levels(gpu):
             assert torch.isfinite(Fb).all()
             assert (Fb[:9] >= 0).all()
     amr.close()
+
+
+@pytest.mark.parametrize("case", ["periodic", "wedge"])
+def test_amr_graph_steps_equal_host_steps(gpu, case):
+    """The graph-captured multi-level step (device dt, one status read per step,
+    recaptured after each regrid) gives the host-driven path's states bit for bit."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import workloads as W
+    if case == "periodic":
+        U, lvd = small_det(periodic=(1, 1))
+        kw = dict(max_level=1, block=16, tag_buffer=1, regrid_interval=3,
+                  tags=dict(box=(lvd["dx"] * 4, lvd["dx"] * 14, -1.0, 1.0), box_only=True))
+    else:
+        U, lvd = W.wedge(nx=64, ny=32)
+        kw = dict(max_level=2, block=16, tag_buffer=2, regrid_interval=4, tags=dict(density_tag=0.05))
+    lv = hf.make_level(**lvd)
+    a = hf.AmrStepper(gpu, lv, cuda(U), **kw)
+    b = hf.AmrStepper(gpu, lv, cuda(U), **kw)
+    b.set_graph(False)
+    for _ in range(9):  # two or three regrids on the way
+        assert a.step(cfl=0.5) == b.step(cfl=0.5)
+    assert a.stats()["graph_steps"] == 9 and b.stats()["graph_steps"] == 0
+    assert a.time == b.time
+    for l in range(kw["max_level"] + 1):
+        Fa, acta = a.level(l)
+        Fb, actb = b.level(l)
+        assert np.array_equal(acta, actb)
+        blk = kw["block"]
+        for bj, bi in zip(*np.nonzero(acta)):
+            sl = (slice(None), slice(bj * blk, (bj + 1) * blk), slice(bi * blk, (bi + 1) * blk))
+            assert torch.equal(Fa[sl], Fb[sl]), (l, bj, bi)
+    a.close()
+    b.close()
