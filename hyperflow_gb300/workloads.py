@@ -12,6 +12,9 @@
   ignition: 4096 0D cells of H2/air (O2 : N2 = 1 : 3.76, the reference's 9 species),
            T ~ U[1000, 1500] K, p ~ U[1, 5] atm, phi ~ U[0.5, 2], for the sensitivity
            (adjoint) runs.
+  sun_cj, teng_case1: the reference's two case configurations
+           (HyperFlow_V3/cases/sun_cj/smoke.json, cases/teng_case1/smoke.json) as one
+           uniform level at their finest resolution.
 The diluent is argon (the inert AR extension species, 10-species mechanism) unless
 diluent="N2" is asked for (9 species, the reference mechanism as is).
 """
@@ -133,3 +136,54 @@ def wedge(nx=512, ny=256, mach=7.0, angle_deg=30.0, T0=300.0, p0=0.1 * 101325.0,
     level = dict(nx=nx, ny=ny, dx=dx, dy=dx, xlo=-x_tip, ylo=0.0, periodic=(0, 0),
                  boundary_lo=("inflow", "wedge"), boundary_hi=("transmissive", "inflow"), inlet=q, wedge_start=0.0)
     return U, level
+
+
+def _air_X(ns=9):
+    """H2:2, O2:1, N2:3.76 by mole, normalised."""
+    X = np.zeros(ns)
+    X[M.SPECIES.index("H2")], X[M.SPECIES.index("O2")], X[M.SPECIES.index("N2")] = 2.0, 1.0, 3.76
+    return X / X.sum()
+
+
+def sun_cj(nx=25000, ny=8):
+    """The Sun-CJ smoke case as one level at its finest resolution (base 6250 x 2 cells on
+    0.5 m x 1.0 m, two levels of ratio 2: dx = 2e-5 m, dy = 0.125 m).  Stoichiometric H2/air
+    at rest at 1 atm / 300 K with a 2 mm hot spot at 90 atm / 3000 K against the reflecting
+    left wall: a cell is hot by the fraction clamp((w - (x - dx/2)) / dx, 0, 1) of its
+    centre x (HyperFlow_V3/src/BlockAMR.cpp:75,87-90, cases/sun_cj/smoke.json); transmissive
+    right, reflecting top and bottom; CFL 0.5 to 1e-7 s.  nx < 25000 keeps the leading
+    nx x 2e-5 m of the domain.  By 1e-7 s the disturbance has reached x = 2.44 mm; every
+    cell beyond it holds the far-field state (at rest, evolving only by its own chemistry),
+    so a cut well past that point leaves the run unchanged.
+    Returns (U (NV, ny, nx), level keys, case dict)."""
+    dx = 0.5 / 25000
+    dy = 1.0 / ny
+    X = _air_X()
+    fresh = M.primitive(300.0, 101325.0, X=X, ns=9)
+    hot = M.primitive(3000.0, 90.0 * 101325.0, X=X, ns=9)
+    U = np.empty((12, ny, nx))
+    for i in range(nx):
+        x = (i + 0.5) * dx
+        f = min(max((0.002 - (x - 0.5 * dx)) / dx, 0.0), 1.0)
+        U[:, :, i] = (f * hot + (1.0 - f) * fresh)[:, None]
+    level = dict(nx=nx, ny=ny, dx=dx, dy=dy, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("transmissive", "reflecting"), inlet=fresh)
+    return U, level, dict(cfl=0.5, end_time=1e-7)
+
+
+def teng_case1(refine=4):
+    """The Teng oblique-detonation case 1 smoke configuration as one level: base 144 x 64
+    cells on 2.304 mm x 1.024 mm from x = -0.128 mm, refined by `refine` (4 = its two
+    levels of ratio 2: dx = dy = 4e-6 m).  Stoichiometric H2/air at 958.1 K / 1.2029 MPa
+    moving at 2737.7 m/s turned 19 degrees toward the wedge (u0 = V cos a, v0 = -V sin a,
+    HyperFlow_V3/src/BlockAMR.cpp:61-66, cases/teng_case1/smoke.json); inflow left and top,
+    wedge bottom from x = 0, transmissive right; CFL 0.6 to 2e-9 s.
+    Returns (U (NV, ny, nx), level keys, case dict)."""
+    nx, ny = 144 * refine, 64 * refine
+    angle = 19.0 * np.arccos(-1.0) / 180.0
+    q = M.primitive(958.1, 1202900.0, X=_air_X(), u=2737.7 * np.cos(angle), v=-2737.7 * np.sin(angle), ns=9)
+    U = np.empty((12, ny, nx))
+    U[:] = q[:, None, None]
+    level = dict(nx=nx, ny=ny, dx=0.002304 / nx, dy=0.001024 / ny, xlo=-0.000128, ylo=0.0, periodic=(0, 0),
+                 boundary_lo=("inflow", "wedge"), boundary_hi=("transmissive", "inflow"), inlet=q, wedge_start=0.0)
+    return U, level, dict(cfl=0.6, end_time=2e-9)

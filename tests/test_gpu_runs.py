@@ -60,3 +60,84 @@ def test_run_case_writes_reference_files(gpu, tmp_path):
     assert abs(b[11] - a[11]) / abs(a[11]) < 1e-12
     hist = np.genfromtxt(tmp_path / "history.csv", names=True, delimiter=",")
     assert len(hist) == s["steps"] + 1
+
+
+def _final_checks(data):
+    """HyperFlow_V3/tests/check_cases.py:45-48 on a state_N.csv read back."""
+    assert all(np.isfinite(data[n]).all() for n in data.dtype.names)
+    Y = np.column_stack([data[n] for n in data.dtype.names if n.startswith("Y_")])
+    assert np.min(Y) >= 0 and np.max(np.abs(Y.sum(1) - 1)) < 1e-12
+    assert all(np.min(data[n]) > 0 for n in ["rho", "p", "T"])
+
+
+def test_sun_cj_smoke_case(gpu, oracle, tmp_path):
+    """The reference's Sun-CJ smoke case on its finest level (25000 x 8 cells): 25 steps to
+    1e-7 s with no retry (HyperFlow_V3/docs/case_checks.json:7,12) and the final checks of
+    tests/check_cases.py:43-48,58,68; then its leading 6 mm against the oracle."""
+    import json
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import output, workloads as W
+    U, lvd, case = W.sun_cj()
+    s = output.run_case(gpu, hf.make_level(**lvd), cuda(U), case["end_time"], str(tmp_path), cfl=case["cfl"],
+                        flux="plain", chem="batched")
+    assert s["steps"] == 25 and s["retries"] == 0 and s["final_time"] == 1e-7
+    first = np.genfromtxt(tmp_path / "state_0.csv", names=True, delimiter=",")
+    final = np.genfromtxt(tmp_path / "state_1.csv", names=True, delimiter=",")
+    _final_checks(final)
+    volume = first["dx"] * first["dy"]
+    hot = np.isclose(first["T"], 3000.0, rtol=1e-10)
+    assert abs(volume.sum() - 0.5) < 1e-13 and abs(volume[hot].sum() - 0.002) < 1e-14
+    a, b = np.array(json.loads((tmp_path / "summary.json").read_text())["initial_conserved_integrals"]), \
+        np.array(s["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-9
+
+    U, lvd, case = W.sun_cj(nx=300, ny=2)
+    st = hf.Stepper(gpu, hf.make_level(**lvd), cuda(U), flux="plain", chem="batched")
+    g = oracle.make_grid(300, 2, lvd["dx"], lvd["dy"], bc_lo=(0, 0), bc_hi=(1, 0), inlet=lvd["inlet"])
+    Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
+    t = 0.0
+    while t < case["end_time"]:
+        dt = min(case["end_time"] - t, oracle.cfl_dt(g, Ug, case["cfl"]))
+        Ug, dta, ok, _ = oracle.strang_step(g, Ug, dt)
+        assert ok == 0 and st.step(dt=dta) == dta
+        t = case["end_time"] if dta >= case["end_time"] - t else t + dta
+    got = st.state().cpu().numpy().transpose(1, 2, 0).reshape(-1, 12)
+    ref = Ug[2:-2, 2:-2].reshape(-1, 12)
+    Tg, Tr = oracle.properties(got)[2], oracle.properties(ref)[2]
+    assert np.max(np.abs(Tg - Tr) / Tr) < 1e-6
+    assert np.max(np.abs(got[:, :9] - ref[:, :9]) / ref[:, :9].sum(1, keepdims=True)) < 1e-8
+    st.close()
+
+
+def test_teng_case1_smoke_case(gpu, oracle, tmp_path):
+    """The reference's Teng case-1 smoke case on its finest level (576 x 256 cells, wedge
+    bottom, inflow left and top): 5 steps to 2e-9 s with no retry
+    (HyperFlow_V3/docs/case_checks.json:38,43), the final checks of
+    tests/check_cases.py:43-48, and the final state against the oracle's run."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import output, workloads as W
+    U, lvd, case = W.teng_case1()
+    s = output.run_case(gpu, hf.make_level(**lvd), cuda(U), case["end_time"], str(tmp_path), cfl=case["cfl"],
+                        flux="plain", chem="batched")
+    assert s["steps"] == 5 and s["retries"] == 0 and s["final_time"] == 2e-9
+    final = np.genfromtxt(tmp_path / "state_1.csv", names=True, delimiter=",")
+    _final_checks(final)
+    assert len(final) == 576 * 256
+    bc = {"reflecting": 0, "transmissive": 1, "inflow": 2, "wedge": 3}
+    g = oracle.make_grid(lvd["nx"], lvd["ny"], lvd["dx"], lvd["dy"], xlo=lvd["xlo"],
+                         bc_lo=tuple(bc[x] for x in lvd["boundary_lo"]), bc_hi=tuple(bc[x] for x in lvd["boundary_hi"]),
+                         inlet=lvd["inlet"], wedge_start=0.0)
+    Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
+    st = hf.Stepper(gpu, hf.make_level(**lvd), cuda(U), flux="plain", chem="batched")
+    t = 0.0
+    while t < case["end_time"]:
+        dt = min(case["end_time"] - t, oracle.cfl_dt(g, Ug, case["cfl"]))
+        Ug, dta, ok, _ = oracle.strang_step(g, Ug, dt)
+        assert ok == 0 and st.step(dt=dta) == dta
+        t = case["end_time"] if dta >= case["end_time"] - t else t + dta
+    got = st.state().cpu().numpy().transpose(1, 2, 0).reshape(-1, 12)
+    ref = Ug[2:-2, 2:-2].reshape(-1, 12)
+    Tg, Tr = oracle.properties(got)[2], oracle.properties(ref)[2]
+    assert np.max(np.abs(Tg - Tr) / Tr) < 1e-6
+    assert np.max(np.abs(got[:, :9] - ref[:, :9]) / ref[:, :9].sum(1, keepdims=True)) < 1e-8
+    st.close()

@@ -1,0 +1,83 @@
+"""The oracle on the reference's two case configurations, against the outcomes the
+reference records for them (HyperFlow_V3/docs/case_checks.json:7,12,38,43): Sun-CJ
+takes 25 steps to 1e-7 s and Teng case 1 takes 5 steps to 2e-9 s, neither with a retry.
+The final states pass the checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
+
+The reference ran both cases on its AMR hierarchy.  Here each case is one level at the
+finest resolution.  The step is the CFL step of the largest wave rate over all levels
+(BlockAMR.cpp:335-346), which the finest level sets where it covers the hot spot or the
+wedge tip.  So the step sequence, and with it the step count, is the same.  The count
+pins the sound speeds and wave speeds of the hot and shocked gas within a few per cent:
+Sun-CJ's 24th step ends 2.5 per cent short of 1e-7 s, Teng's 4th step 2.3 per cent short
+of 2e-9 s."""
+import numpy as np
+import pytest
+
+
+def run(oracle, U, lvd, case):
+    """BlockAMR::run on one level (BlockAMR.cpp:408-416): the CFL step shortened to land
+    on the end time; returns (final ghosted state, step sizes, rollbacks)."""
+    bc = {"reflecting": 0, "transmissive": 1, "inflow": 2, "wedge": 3}
+    g = oracle.make_grid(lvd["nx"], lvd["ny"], lvd["dx"], lvd["dy"], xlo=lvd.get("xlo", 0.0),
+                         ylo=lvd.get("ylo", 0.0), periodic=lvd["periodic"],
+                         bc_lo=tuple(bc[b] for b in lvd["boundary_lo"]),
+                         bc_hi=tuple(bc[b] for b in lvd["boundary_hi"]), inlet=lvd["inlet"],
+                         wedge_start=lvd.get("wedge_start", 0.0))
+    Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
+    t, end, dts, rollbacks = 0.0, case["end_time"], [], 0
+    while t < end:
+        dt = min(end - t, oracle.cfl_dt(g, Ug, case["cfl"]))
+        Ug, dta, st, _ = oracle.strang_step(g, Ug, dt)
+        assert st == 0
+        rollbacks += dta != dt
+        t = end if dta >= end - t else t + dta
+        dts.append(dta)
+    assert t == end
+    return Ug[2:-2, 2:-2], dts, rollbacks
+
+
+def final_checks(oracle, F):
+    """check_cases.py:45-48: finite, Y_k >= 0 summing to 1 within 1e-12, rho, p, T > 0."""
+    q = F.reshape(-1, F.shape[-1])
+    assert np.all(np.isfinite(q))
+    rho = q[:, :9].sum(1)
+    Y = q[:, :9] / rho[:, None]
+    assert np.min(Y) >= 0 and np.max(np.abs(Y.sum(1) - 1)) < 1e-12
+    p, _, T, st = oracle.properties(q)
+    assert not np.any(st)
+    assert rho.min() > 0 and p.min() > 0 and T.min() > 0
+
+
+@pytest.fixture(scope="module")
+def W():
+    from hyperflow_gb300 import workloads
+    return workloads
+
+
+def test_sun_cj_smoke_case(oracle, W):
+    """The leading 6 mm of the 0.5 m domain (the disturbance reaches 2.44 mm)."""
+    U, lvd, case = W.sun_cj(nx=300, ny=2)
+    F, dts, rollbacks = run(oracle, U, lvd, case)
+    assert len(dts) == 25 and rollbacks == 0
+    final_checks(oracle, F)
+    T0 = oracle.properties(U.transpose(1, 2, 0).reshape(-1, 12))[2]
+    hot = np.isclose(T0, 3000.0, rtol=1e-10)
+    # check_cases.py:58: the hot spot is 0.002 m^3 per unit depth (2 mm x 1 m)
+    assert abs(hot.sum() * lvd["dx"] * lvd["dy"] - 0.002) < 1e-14
+    # check_cases.py:68: mass and energy relative change (closed but for the far right
+    # face, where the gas is at rest)
+    a = U.transpose(1, 2, 0).reshape(-1, 12).sum(0)
+    b = F.reshape(-1, 12).sum(0)
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11
+    assert abs(b[11] / a[11] - 1) < 1e-9
+    # the cut: every cell past the disturbance holds the far-field state
+    far = np.nonzero(np.any(F != F[:, -1:], axis=(0, 2)))[0].max()
+    assert (far + 1) * lvd["dx"] < 0.003
+
+
+def test_teng_case1_smoke_case(oracle, W):
+    U, lvd, case = W.teng_case1()
+    assert (lvd["nx"], lvd["ny"]) == (576, 256) and abs(lvd["dx"] - 4e-6) < 1e-18
+    F, dts, rollbacks = run(oracle, U, lvd, case)
+    assert len(dts) == 5 and rollbacks == 0
+    final_checks(oracle, F)
