@@ -15,6 +15,8 @@
   sun_cj, teng_case1: the reference's two case configurations
            (HyperFlow_V3/cases/sun_cj/smoke.json, cases/teng_case1/smoke.json) as one
            uniform level at their finest resolution.
+  blast2d: the inert and reacting blast checks of HyperFlow_V3/tests/validate.py as one
+           uniform level at their finest resolution.
 The diluent is argon (the inert AR extension species, 10-species mechanism) unless
 diluent="N2" is asked for (9 species, the reference mechanism as is).
 """
@@ -187,3 +189,40 @@ def teng_case1(refine=4):
     level = dict(nx=nx, ny=ny, dx=0.002304 / nx, dy=0.001024 / ny, xlo=-0.000128, ylo=0.0, periodic=(0, 0),
                  boundary_lo=("inflow", "wedge"), boundary_hi=("transmissive", "inflow"), inlet=q, wedge_start=0.0)
     return U, level, dict(cfl=0.6, end_time=2e-9)
+
+
+def blast2d(reacting=True):
+    """A disc of stoichiometric H2/air at 1500 K / 10 atm in the same mixture at rest at
+    300 K / 1 atm, closed by reflecting walls; each cell is the 4 x 4-point average of the
+    disc indicator (HyperFlow_V3/src/BlockAMR.cpp:69,97-121).  One level at the finest
+    resolution of the reference's checks:
+      reacting=False: tests/validate.py:122-129, 0.02 m square, base 24 x 24 with two
+                      levels (96 x 96), centre (0.01, 0.01), radius 2 mm, no chemistry,
+                      output at 1e-6 and 2e-6 s;
+      reacting=True:  tests/validate.py:174-179, 0.01 m square, base 16 x 16 with one
+                      level (32 x 32), centre (0.005, 0.005), radius 1.5 mm, chemistry,
+                      output at 1e-7 and 2e-7 s.
+    CFL 0.6.  Returns (U (NV, n, n), level keys, case dict)."""
+    if reacting:
+        n, length, centre, radius, times = 32, 0.01, 0.005, 0.0015, [1e-7, 2e-7]
+    else:
+        n, length, centre, radius, times = 96, 0.02, 0.01, 0.002, [1e-6, 2e-6]
+    X = _air_X()
+    fresh = M.primitive(300.0, 101325.0, X=X, ns=9)
+    hot = M.primitive(1500.0, 10.0 * 101325.0, X=X, ns=9)
+    dx = length / n
+    quad = 4
+    U = np.empty((12, n, n))
+    for j in range(n):
+        for i in range(n):
+            x, y = (i + 0.5) * dx, (j + 0.5) * dx
+            acc = np.zeros(12)
+            for b in range(quad):
+                for a in range(quad):
+                    xx = x + dx * ((a + 0.5) / quad - 0.5)
+                    yy = y + dx * ((b + 0.5) / quad - 0.5)
+                    acc += hot if np.hypot(xx - centre, yy - centre) < radius else fresh
+            U[:, j, i] = acc / (quad * quad)
+    level = dict(nx=n, ny=n, dx=dx, dy=dx, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("reflecting", "reflecting"), inlet=fresh)
+    return U, level, dict(cfl=0.6, end_time=times[-1], output_times=times, chemistry=reacting)

@@ -141,3 +141,46 @@ def test_teng_case1_smoke_case(gpu, oracle, tmp_path):
     assert np.max(np.abs(Tg - Tr) / Tr) < 1e-6
     assert np.max(np.abs(got[:, :9] - ref[:, :9]) / ref[:, :9].sum(1, keepdims=True)) < 1e-8
     st.close()
+
+
+def _stepper_run(gpu, U, lvd, case):
+    """BlockAMR::run (BlockAMR.cpp:400-416) on the GPU stepper: the device CFL step
+    shortened to land on each output time; returns (final state (ny*nx, NV), step sizes)."""
+    import hyperflow_gb300 as hf
+    st = hf.Stepper(gpu, hf.make_level(**lvd), cuda(U), chemistry=case["chemistry"], flux="plain", chem="batched")
+    t, dts = 0.0, []
+    for target in case["output_times"]:
+        while t < target:
+            dt = st.step(dt=min(target - t, st.cfl_dt(case["cfl"])), cfl=case["cfl"])
+            t = target if dt >= target - t else t + dt
+            dts.append(dt)
+    out = st.state().cpu().numpy().transpose(1, 2, 0).reshape(-1, U.shape[0])
+    st.close()
+    return out, dts
+
+
+def test_blast2d_checks(gpu, oracle):
+    """The reference's blast checks on one level at their finest resolution: the inert
+    blast takes 37 steps to 2e-6 s and the reacting blast ends with a peak Y_H + Y_O + Y_OH
+    of 1.4893699370443747e-07 (HyperFlow_V3/docs/amr_checks.json:52,101); both against
+    the oracle's runs."""
+    from hyperflow_gb300 import workloads as W
+    for reacting in (False, True):
+        U, lvd, case = W.blast2d(reacting=reacting)
+        got, dts = _stepper_run(gpu, U, lvd, case)
+        g = oracle.make_grid(lvd["nx"], lvd["ny"], lvd["dx"], lvd["dy"], bc_lo=(0, 0), bc_hi=(0, 0))
+        Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
+        for dt in dts:
+            Ug, dta, ok, _ = oracle.strang_step(g, Ug, dt, chemistry=reacting)
+            assert ok == 0 and dta == dt
+        ref = Ug[2:-2, 2:-2].reshape(-1, 12)
+        Tg, Tr = oracle.properties(got)[2], oracle.properties(ref)[2]
+        assert np.max(np.abs(Tg - Tr) / Tr) < 1e-6
+        assert np.max(np.abs(got[:, :9] - ref[:, :9]) / ref[:, :9].sum(1, keepdims=True)) < 1e-8
+        if reacting:
+            assert dts == [1e-7, 1e-7]
+            S = oracle.SPECIES
+            peak = np.max((got[:, S.index("H")] + got[:, S.index("O")] + got[:, S.index("OH")]) / got[:, :9].sum(1))
+            assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
+        else:
+            assert len(dts) == 37

@@ -1,7 +1,10 @@
-"""The oracle on the reference's two case configurations, against the outcomes the
-reference records for them (HyperFlow_V3/docs/case_checks.json:7,12,38,43): Sun-CJ
-takes 25 steps to 1e-7 s and Teng case 1 takes 5 steps to 2e-9 s, neither with a retry.
-The final states pass the checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
+"""The oracle on the reference's case configurations and blast checks, against the
+outcomes the reference records for them:
+- HyperFlow_V3/docs/case_checks.json:7,12,38,43: Sun-CJ takes 25 steps to 1e-7 s and
+  Teng case 1 takes 5 steps to 2e-9 s, neither with a retry.  The final states pass the
+  checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
+- HyperFlow_V3/docs/amr_checks.json:52,101: the inert blast takes 37 steps to 2e-6 s, and
+  the reacting blast ends with a peak Y_H + Y_O + Y_OH of 1.4893699370443747e-07.
 
 The reference ran both cases on its AMR hierarchy.  Here each case is one level at the
 finest resolution.  The step is the CFL step of the largest wave rate over all levels
@@ -9,14 +12,16 @@ finest resolution.  The step is the CFL step of the largest wave rate over all l
 wedge tip.  So the step sequence, and with it the step count, is the same.  The count
 pins the sound speeds and wave speeds of the hot and shocked gas within a few per cent:
 Sun-CJ's 24th step ends 2.5 per cent short of 1e-7 s, Teng's 4th step 2.3 per cent short
-of 2e-9 s."""
+of 2e-9 s.  The peak radical fraction of the reacting blast pins far more: the induction
+chemistry at 1500 K / 10 atm over 2e-7 s, with the slight cooling that the flux scheme
+brings to the disc centre (a 0D reactor alone gives 5.5e-5 more)."""
 import numpy as np
 import pytest
 
 
 def run(oracle, U, lvd, case):
-    """BlockAMR::run on one level (BlockAMR.cpp:408-416): the CFL step shortened to land
-    on the end time; returns (final ghosted state, step sizes, rollbacks)."""
+    """BlockAMR::run on one level (BlockAMR.cpp:400-416): the CFL step shortened to land
+    on each output time; returns (final interior state, step sizes, rollbacks)."""
     bc = {"reflecting": 0, "transmissive": 1, "inflow": 2, "wedge": 3}
     g = oracle.make_grid(lvd["nx"], lvd["ny"], lvd["dx"], lvd["dy"], xlo=lvd.get("xlo", 0.0),
                          ylo=lvd.get("ylo", 0.0), periodic=lvd["periodic"],
@@ -24,15 +29,16 @@ def run(oracle, U, lvd, case):
                          bc_hi=tuple(bc[b] for b in lvd["boundary_hi"]), inlet=lvd["inlet"],
                          wedge_start=lvd.get("wedge_start", 0.0))
     Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
-    t, end, dts, rollbacks = 0.0, case["end_time"], [], 0
-    while t < end:
-        dt = min(end - t, oracle.cfl_dt(g, Ug, case["cfl"]))
-        Ug, dta, st, _ = oracle.strang_step(g, Ug, dt)
-        assert st == 0
-        rollbacks += dta != dt
-        t = end if dta >= end - t else t + dta
-        dts.append(dta)
-    assert t == end
+    t, dts, rollbacks = 0.0, [], 0
+    for target in case.get("output_times", [case["end_time"]]):
+        while t < target:
+            dt = min(target - t, oracle.cfl_dt(g, Ug, case["cfl"]))
+            Ug, dta, st, _ = oracle.strang_step(g, Ug, dt, chemistry=case.get("chemistry", True))
+            assert st == 0
+            rollbacks += dta != dt
+            t = target if dta >= target - t else t + dta
+            dts.append(dta)
+    assert t == case["end_time"]
     return Ug[2:-2, 2:-2], dts, rollbacks
 
 
@@ -81,3 +87,30 @@ def test_teng_case1_smoke_case(oracle, W):
     F, dts, rollbacks = run(oracle, U, lvd, case)
     assert len(dts) == 5 and rollbacks == 0
     final_checks(oracle, F)
+
+
+def test_blast2d_inert_check(oracle, W):
+    """validate.py:122-137: 37 steps, no retry, mass and energy within 1e-11, a pressure
+    field symmetric under the transpose."""
+    U, lvd, case = W.blast2d(reacting=False)
+    F, dts, rollbacks = run(oracle, U, lvd, case)
+    assert len(dts) == 37 and rollbacks == 0
+    final_checks(oracle, F)
+    a, b = U.transpose(1, 2, 0).reshape(-1, 12).sum(0), F.reshape(-1, 12).sum(0)
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+    p = oracle.properties(F.reshape(-1, 12))[0].reshape(F.shape[:2])
+    assert np.mean(np.abs(p - p.T)) / np.mean(p) < 1e-12
+
+
+def test_blast2d_reacting_peak_radicals(oracle, W):
+    """validate.py:174-191: two steps of 1e-7 s, no retry, and the peak of
+    Y_H + Y_O + Y_OH recorded as 1.4893699370443747e-07 (the oracle: 4.6e-7 below it;
+    the reference integrates with CVODE on an AMR hierarchy)."""
+    U, lvd, case = W.blast2d(reacting=True)
+    F, dts, rollbacks = run(oracle, U, lvd, case)
+    assert dts == [1e-7, 1e-7] and rollbacks == 0
+    final_checks(oracle, F)
+    q = F.reshape(-1, 12)
+    S = oracle.SPECIES
+    peak = np.max((q[:, S.index("H")] + q[:, S.index("O")] + q[:, S.index("OH")]) / q[:, :9].sum(1))
+    assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
