@@ -15,8 +15,8 @@
   sun_cj, teng_case1: the reference's two case configurations
            (HyperFlow_V3/cases/sun_cj/smoke.json, cases/teng_case1/smoke.json) as one
            uniform level at their finest resolution.
-  blast2d: the inert and reacting blast checks of HyperFlow_V3/tests/validate.py as one
-           uniform level at their finest resolution.
+  blast2d, entropy_wave: the blast and moving-refinement checks of
+           HyperFlow_V3/tests/validate.py as one uniform level at their finest resolution.
 The diluent is argon (the inert AR extension species, 10-species mechanism) unless
 diluent="N2" is asked for (9 species, the reference mechanism as is).
 """
@@ -226,3 +226,32 @@ def blast2d(reacting=True):
     level = dict(nx=n, ny=n, dx=dx, dy=dx, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
                  boundary_hi=("reflecting", "reflecting"), inlet=fresh)
     return U, level, dict(cfl=0.6, end_time=times[-1], output_times=times, chemistry=reacting)
+
+
+def entropy_wave():
+    """A Gaussian temperature dip (T = 300 K / (1 + 0.2 exp(-r^2 / sigma^2)), sigma 0.7 mm,
+    centre (3 mm, 4 mm)) at 1 atm in stoichiometric H2/air moving at (300, 200) m/s through
+    a periodic 0.01 m square; each cell is the 4 x 4-point average of the state
+    (HyperFlow_V3/src/BlockAMR.cpp:97-110).  The moving-refinement check of
+    tests/validate.py:104-119 (base 16 x 16 with two levels) on one level of 64 x 64 cells;
+    no chemistry, CFL 0.6, output at 2e-6 and 4e-6 s.
+    Returns (U (NV, 64, 64), level keys, case dict)."""
+    n, length, quad = 64, 0.01, 4
+    cx, cy, sigma, amp = 0.003, 0.004, 0.0007, 0.2
+    X = _air_X()
+    dx = length / n
+    U = np.empty((12, n, n))
+    for j in range(n):
+        for i in range(n):
+            x, y = (i + 0.5) * dx, (j + 0.5) * dx
+            acc = np.zeros(12)
+            for b in range(quad):
+                for a in range(quad):
+                    xx = x + dx * ((a + 0.5) / quad - 0.5)
+                    yy = y + dx * ((b + 0.5) / quad - 0.5)
+                    bump = 1.0 + amp * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) / (sigma * sigma))
+                    acc += M.primitive(300.0 / bump, 101325.0, X=X, u=300.0, v=200.0, ns=9)
+            U[:, j, i] = acc / (quad * quad)
+    level = dict(nx=n, ny=n, dx=dx, dy=dx, periodic=(1, 1), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("transmissive", "reflecting"), inlet=M.primitive(300.0, 101325.0, X=X, ns=9))
+    return U, level, dict(cfl=0.6, end_time=4e-6, output_times=[2e-6, 4e-6], chemistry=False)

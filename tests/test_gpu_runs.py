@@ -184,3 +184,20 @@ def test_blast2d_checks(gpu, oracle):
             assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
         else:
             assert len(dts) == 37
+
+
+def test_entropy_wave_check(gpu, oracle):
+    """The reference's moving-refinement check on one 64 x 64 level: 58 steps to 4e-6 s
+    (HyperFlow_V3/docs/amr_checks.json:35), against the oracle's run."""
+    from hyperflow_gb300 import workloads as W
+    U, lvd, case = W.entropy_wave()
+    got, dts = _stepper_run(gpu, U, lvd, case)
+    assert len(dts) == 58
+    g = oracle.make_grid(64, 64, lvd["dx"], lvd["dy"], periodic=(1, 1))
+    Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
+    for dt in dts:
+        Ug, dta, ok, _ = oracle.strang_step(g, Ug, dt, chemistry=False)
+        assert ok == 0 and dta == dt
+    ref = Ug[2:-2, 2:-2].reshape(-1, 12)
+    import helpers as H
+    assert H.comp_err(got, ref) < 1e-10

@@ -3,8 +3,9 @@ outcomes the reference records for them:
 - HyperFlow_V3/docs/case_checks.json:7,12,38,43: Sun-CJ takes 25 steps to 1e-7 s and
   Teng case 1 takes 5 steps to 2e-9 s, neither with a retry.  The final states pass the
   checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
-- HyperFlow_V3/docs/amr_checks.json:52,101: the inert blast takes 37 steps to 2e-6 s, and
-  the reacting blast ends with a peak Y_H + Y_O + Y_OH of 1.4893699370443747e-07.
+- HyperFlow_V3/docs/amr_checks.json:35,52,101: the moving entropy wave takes 58 steps to
+  4e-6 s, the inert blast 37 steps to 2e-6 s, and the reacting blast ends with a peak
+  Y_H + Y_O + Y_OH of 1.4893699370443747e-07.
 
 The reference ran both cases on its AMR hierarchy.  Here each case is one level at the
 finest resolution.  The step is the CFL step of the largest wave rate over all levels
@@ -114,3 +115,13 @@ def test_blast2d_reacting_peak_radicals(oracle, W):
     S = oracle.SPECIES
     peak = np.max((q[:, S.index("H")] + q[:, S.index("O")] + q[:, S.index("OH")]) / q[:, :9].sum(1))
     assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
+
+
+def test_entropy_wave_check(oracle, W):
+    """validate.py:104-119: 58 steps, no retry, mass and energy within 1e-11 (periodic)."""
+    U, lvd, case = W.entropy_wave()
+    F, dts, rollbacks = run(oracle, U, lvd, case)
+    assert len(dts) == 58 and rollbacks == 0
+    final_checks(oracle, F)
+    a, b = U.transpose(1, 2, 0).reshape(-1, 12).sum(0), F.reshape(-1, 12).sum(0)
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
