@@ -1,0 +1,37 @@
+"""Writes reference_records.json: the run outcomes that HyperFlow V3 records for its own
+checks (HyperFlow_V3/docs/case_checks.json and docs/amr_checks.json), reduced to the
+fields the oracle and GPU tests compare with.  Run where the reference tree is present:
+
+    python tests/golden/make_reference_records.py /root/reference/HyperFlow_V3
+"""
+import json
+import os
+import sys
+
+FIELDS = {
+    ("case_checks.json", "cases", "sun_cj"): ["final_time_s", "steps", "retries", "dx_min_m", "dy_min_m",
+                                              "initial_hotspot_volume_m3", "mass_relative_change",
+                                              "energy_relative_change"],
+    ("case_checks.json", "cases", "teng_case1"): ["final_time_s", "steps", "retries", "dx_min_m", "dy_min_m"],
+    ("amr_checks.json", "tests", "moving_refine_coarsen"): ["steps"],
+    ("amr_checks.json", "tests", "blast2d_inert"): ["steps", "transpose_pressure_error"],
+    ("amr_checks.json", "tests", "blast2d_reacting"): ["peak_radical_mass_fraction", "steps", "retries",
+                                                       "first_order_stages"],
+}
+
+
+def main(root):
+    out = {}
+    for (name, group, case), keys in FIELDS.items():
+        with open(os.path.join(root, "docs", name)) as f:
+            rec = json.load(f)[group][case]
+        out[case] = {"source": "HyperFlow_V3/docs/" + name, **{k: rec[k] for k in keys}}
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_records.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+        f.write("\n")
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/HyperFlow_V3")

@@ -96,3 +96,12 @@ def chem_cells(n, seed=0):
     """(NV, n) independent 0D cells of uneven stiffness, N2 diluent (9 species)."""
     from hyperflow_gb300 import workloads as W
     return W.chem_batch(n, seed=seed, diluent="N2")[0]
+
+
+def reference_records():
+    """Run outcomes the reference records for its own checks (tests/golden/
+    reference_records.json, written by tests/golden/make_reference_records.py)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_records.json")) as f:
+        return json.load(f)

@@ -10,6 +10,8 @@ import numpy as np
 import pytest
 import torch
 
+import helpers as H
+
 pytestmark = pytest.mark.gpu
 
 
@@ -80,13 +82,14 @@ def test_sun_cj_smoke_case(gpu, oracle, tmp_path):
     U, lvd, case = W.sun_cj()
     s = output.run_case(gpu, hf.make_level(**lvd), cuda(U), case["end_time"], str(tmp_path), cfl=case["cfl"],
                         flux="plain", chem="batched")
-    assert s["steps"] == 25 and s["retries"] == 0 and s["final_time"] == 1e-7
+    R = H.reference_records()["sun_cj"]
+    assert s["steps"] == R["steps"] and s["retries"] == R["retries"] and s["final_time"] == R["final_time_s"]
     first = np.genfromtxt(tmp_path / "state_0.csv", names=True, delimiter=",")
     final = np.genfromtxt(tmp_path / "state_1.csv", names=True, delimiter=",")
     _final_checks(final)
     volume = first["dx"] * first["dy"]
     hot = np.isclose(first["T"], 3000.0, rtol=1e-10)
-    assert abs(volume.sum() - 0.5) < 1e-13 and abs(volume[hot].sum() - 0.002) < 1e-14
+    assert abs(volume.sum() - 0.5) < 1e-13 and abs(volume[hot].sum() - R["initial_hotspot_volume_m3"]) < 1e-14
     a, b = np.array(json.loads((tmp_path / "summary.json").read_text())["initial_conserved_integrals"]), \
         np.array(s["final_conserved_integrals"])
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-9
@@ -119,7 +122,8 @@ def test_teng_case1_smoke_case(gpu, oracle, tmp_path):
     U, lvd, case = W.teng_case1()
     s = output.run_case(gpu, hf.make_level(**lvd), cuda(U), case["end_time"], str(tmp_path), cfl=case["cfl"],
                         flux="plain", chem="batched")
-    assert s["steps"] == 5 and s["retries"] == 0 and s["final_time"] == 2e-9
+    R = H.reference_records()["teng_case1"]
+    assert s["steps"] == R["steps"] and s["retries"] == R["retries"] and s["final_time"] == R["final_time_s"]
     final = np.genfromtxt(tmp_path / "state_1.csv", names=True, delimiter=",")
     _final_checks(final)
     assert len(final) == 576 * 256
@@ -165,6 +169,7 @@ def test_blast2d_checks(gpu, oracle):
     of 1.4893699370443747e-07 (HyperFlow_V3/docs/amr_checks.json:52,101); both against
     the oracle's runs."""
     from hyperflow_gb300 import workloads as W
+    R = H.reference_records()
     for reacting in (False, True):
         U, lvd, case = W.blast2d(reacting=reacting)
         got, dts = _stepper_run(gpu, U, lvd, case)
@@ -178,12 +183,12 @@ def test_blast2d_checks(gpu, oracle):
         assert np.max(np.abs(Tg - Tr) / Tr) < 1e-6
         assert np.max(np.abs(got[:, :9] - ref[:, :9]) / ref[:, :9].sum(1, keepdims=True)) < 1e-8
         if reacting:
-            assert dts == [1e-7, 1e-7]
+            assert dts == [1e-7] * R["blast2d_reacting"]["steps"]
             S = oracle.SPECIES
             peak = np.max((got[:, S.index("H")] + got[:, S.index("O")] + got[:, S.index("OH")]) / got[:, :9].sum(1))
-            assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
+            assert abs(peak / R["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6
         else:
-            assert len(dts) == 37
+            assert len(dts) == R["blast2d_inert"]["steps"]
 
 
 def test_entropy_wave_check(gpu, oracle):
@@ -192,12 +197,11 @@ def test_entropy_wave_check(gpu, oracle):
     from hyperflow_gb300 import workloads as W
     U, lvd, case = W.entropy_wave()
     got, dts = _stepper_run(gpu, U, lvd, case)
-    assert len(dts) == 58
+    assert len(dts) == H.reference_records()["moving_refine_coarsen"]["steps"]
     g = oracle.make_grid(64, 64, lvd["dx"], lvd["dy"], periodic=(1, 1))
     Ug = oracle.fill_ghosts(g, oracle.ghosted(np.ascontiguousarray(U.transpose(1, 2, 0))))
     for dt in dts:
         Ug, dta, ok, _ = oracle.strang_step(g, Ug, dt, chemistry=False)
         assert ok == 0 and dta == dt
     ref = Ug[2:-2, 2:-2].reshape(-1, 12)
-    import helpers as H
     assert H.comp_err(got, ref) < 1e-10

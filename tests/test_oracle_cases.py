@@ -1,5 +1,5 @@
 """The oracle on the reference's case configurations and blast checks, against the
-outcomes the reference records for them:
+outcomes the reference records for them (tests/golden/reference_records.json):
 - HyperFlow_V3/docs/case_checks.json:7,12,38,43: Sun-CJ takes 25 steps to 1e-7 s and
   Teng case 1 takes 5 steps to 2e-9 s, neither with a retry.  The final states pass the
   checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
@@ -18,6 +18,10 @@ chemistry at 1500 K / 10 atm over 2e-7 s, with the slight cooling that the flux 
 brings to the disc centre (a 0D reactor alone gives 5.5e-5 more)."""
 import numpy as np
 import pytest
+
+import helpers as H
+
+REC = H.reference_records()
 
 
 def run(oracle, U, lvd, case):
@@ -65,12 +69,12 @@ def test_sun_cj_smoke_case(oracle, W):
     """The leading 6 mm of the 0.5 m domain (the disturbance reaches 2.44 mm)."""
     U, lvd, case = W.sun_cj(nx=300, ny=2)
     F, dts, rollbacks = run(oracle, U, lvd, case)
-    assert len(dts) == 25 and rollbacks == 0
+    assert len(dts) == REC["sun_cj"]["steps"] and rollbacks == REC["sun_cj"]["retries"]
     final_checks(oracle, F)
     T0 = oracle.properties(U.transpose(1, 2, 0).reshape(-1, 12))[2]
     hot = np.isclose(T0, 3000.0, rtol=1e-10)
     # check_cases.py:58: the hot spot is 0.002 m^3 per unit depth (2 mm x 1 m)
-    assert abs(hot.sum() * lvd["dx"] * lvd["dy"] - 0.002) < 1e-14
+    assert abs(hot.sum() * lvd["dx"] * lvd["dy"] - REC["sun_cj"]["initial_hotspot_volume_m3"]) < 1e-14
     # check_cases.py:68: mass and energy relative change (closed but for the far right
     # face, where the gas is at rest)
     a = U.transpose(1, 2, 0).reshape(-1, 12).sum(0)
@@ -86,7 +90,7 @@ def test_teng_case1_smoke_case(oracle, W):
     U, lvd, case = W.teng_case1()
     assert (lvd["nx"], lvd["ny"]) == (576, 256) and abs(lvd["dx"] - 4e-6) < 1e-18
     F, dts, rollbacks = run(oracle, U, lvd, case)
-    assert len(dts) == 5 and rollbacks == 0
+    assert len(dts) == REC["teng_case1"]["steps"] and rollbacks == REC["teng_case1"]["retries"]
     final_checks(oracle, F)
 
 
@@ -95,7 +99,7 @@ def test_blast2d_inert_check(oracle, W):
     field symmetric under the transpose."""
     U, lvd, case = W.blast2d(reacting=False)
     F, dts, rollbacks = run(oracle, U, lvd, case)
-    assert len(dts) == 37 and rollbacks == 0
+    assert len(dts) == REC["blast2d_inert"]["steps"] and rollbacks == 0
     final_checks(oracle, F)
     a, b = U.transpose(1, 2, 0).reshape(-1, 12).sum(0), F.reshape(-1, 12).sum(0)
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
@@ -109,19 +113,19 @@ def test_blast2d_reacting_peak_radicals(oracle, W):
     the reference integrates with CVODE on an AMR hierarchy)."""
     U, lvd, case = W.blast2d(reacting=True)
     F, dts, rollbacks = run(oracle, U, lvd, case)
-    assert dts == [1e-7, 1e-7] and rollbacks == 0
+    assert dts == [1e-7] * REC["blast2d_reacting"]["steps"] and rollbacks == REC["blast2d_reacting"]["retries"]
     final_checks(oracle, F)
     q = F.reshape(-1, 12)
     S = oracle.SPECIES
     peak = np.max((q[:, S.index("H")] + q[:, S.index("O")] + q[:, S.index("OH")]) / q[:, :9].sum(1))
-    assert abs(peak / 1.4893699370443747e-07 - 1) < 5e-6
+    assert abs(peak / REC["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6
 
 
 def test_entropy_wave_check(oracle, W):
     """validate.py:104-119: 58 steps, no retry, mass and energy within 1e-11 (periodic)."""
     U, lvd, case = W.entropy_wave()
     F, dts, rollbacks = run(oracle, U, lvd, case)
-    assert len(dts) == 58 and rollbacks == 0
+    assert len(dts) == REC["moving_refine_coarsen"]["steps"] and rollbacks == 0
     final_checks(oracle, F)
     a, b = U.transpose(1, 2, 0).reshape(-1, 12).sum(0), F.reshape(-1, 12).sum(0)
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
