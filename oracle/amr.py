@@ -3,8 +3,8 @@ import it; the GPU package never does.
 
 A restatement, with the oracle's per-cell functions, of the multi-level stepper's
 algorithm at refinement ratio 2 without time subcycling (HyperFlow_V3/src/BlockAMR.cpp:
-euler :202-264, flow :266-270, react :271-285).  Scope: two levels, periodic in x and
-y, a fixed set of active level-1 blocks (no regrid).
+euler :202-264, flow :266-270, react :271-285, regrid :367-373 with ErrorEst :170-200).
+Scope: two levels, periodic in x and y.
 - Ghosts: level 0 by the periodic fill; level 1 by the periodic images of its dense
   array, then, in each active block's 2-cell frame part that lies in an inactive block
   (across a periodic edge: the inactive periodic image), ConservativeInterp from level 0
@@ -15,6 +15,14 @@ y, a fixed set of active level-1 blocks (no regrid).
 - flow(h): two stages, Heun combination, average_down, validation.
 - react(dt): the leaf cells of both levels (level-0 cells under no active block, every
   active level-1 cell) through the oracle's ChemistryBatch, then average_down.
+- regrid (every regrid_interval steps, and once to build the initial hierarchy from the
+  base level alone): ErrorEst tags of level 0; a level-1 block is active when a tagged
+  cell lies in its level-0 footprint grown by tag_buffer cells (wrapping across the
+  periodic edges; proper nesting always holds under a fully active level 0).  Blocks
+  that become active are filled by ConservativeInterp from level 0; blocks that stay
+  keep their data; nothing is averaged.  The leaf totals must survive the remap to 1e-8
+  of the total of the magnitudes (regridChecked, :369-371).  The block rule is the GPU
+  stepper's deterministic choice in place of AMReX's clustering.
 States are AoS arrays (..., NS+3); levels are dense ghosted arrays (ny+4, nx+4, NV).
 """
 import numpy as np
@@ -22,10 +30,26 @@ import numpy as np
 import oracle
 
 
+def criteria(pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0, chemistry=True,
+             box=None, box_only=False, velocity=(0.0, 0.0)):
+    """ErrorEst criteria from the reference's case keys (BlockAMR.cpp:170-200 defaults)."""
+    c = oracle.TagCriteria()
+    c.pressure_tag, c.temperature_tag, c.fuel_rate_tag, c.density_tag = (pressure_tag, temperature_tag,
+                                                                         fuel_rate_tag, density_tag)
+    c.chemistry, c.box_only, c.has_box = int(bool(chemistry)), int(bool(box_only)), int(box is not None)
+    if box is not None:
+        for k in range(4):
+            c.box[k] = float(box[k])
+    c.velocity[0], c.velocity[1] = float(velocity[0]), float(velocity[1])
+    return c
+
+
 class AmrOracle:
-    def __init__(self, U0, U1, active, dx, dy, block, chemistry=True, rtol=1e-8, atol=1e-15):
+    def __init__(self, U0, U1, active, dx, dy, block, chemistry=True, rtol=1e-8, atol=1e-15, crit=None,
+                 tag_buffer=1, regrid_interval=0):
         """U0: (ny, nx, NV) level 0; U1: (2ny, 2nx, NV) level 1 (read in active blocks);
-        active: (nby, nbx) uint8 of level-1 blocks (block x block fine cells)."""
+        active: (nby, nbx) uint8 of level-1 blocks (block x block fine cells); crit:
+        criteria(...) for regrids."""
         ny, nx, nv = U0.shape
         if U1.shape != (2 * ny, 2 * nx, nv):
             raise ValueError("level 1 must be the level-0 domain at ratio 2")
@@ -37,6 +61,8 @@ class AmrOracle:
             raise ValueError("blocks must tile level 1")
         self.blocks = [(bi, bj) for bj in range(nby) for bi in range(nbx) if self.active[bj, bi]]
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
+        self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
+        self.time, self.steps, self.regrids = 0.0, 0, 0
         self.g0 = oracle.make_grid(nx, ny, dx, dy, periodic=(1, 1))
         self.g1 = oracle.make_grid(2 * nx, 2 * ny, dx / 2, dy / 2, periodic=(1, 1))
         # one block as its own box: transmissive sides (no wall faces in a periodic domain)
@@ -44,6 +70,17 @@ class AmrOracle:
         self.X = [oracle.ghosted(np.array(U0, dtype=np.float64)), oracle.ghosted(np.array(U1, dtype=np.float64))]
         self.regions = self._regions()
         self.X[0][2:-2, 2:-2] = self._averaged(self.X[1], self.X[0])[2:-2, 2:-2]
+
+    @classmethod
+    def from_base(cls, U0, dx, dy, block, crit, tag_buffer=1, regrid_interval=0, **kw):
+        """The hierarchy the GPU stepper builds from the base level alone: level 0 = U0,
+        then one regrid (hf_amr_create)."""
+        ny, nx, nv = U0.shape
+        o = cls(U0, np.zeros((2 * ny, 2 * nx, nv)), np.zeros((2 * ny // block, 2 * nx // block), np.uint8), dx, dy,
+                block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval, **kw)
+        o.regrid()
+        o.regrids = 0
+        return o
 
     # ------------------------------------------------------------ hierarchy
     def _regions(self):
@@ -168,14 +205,50 @@ class AmrOracle:
         self.flow(0.5 * dt)
         self.react(dt)
         self.flow(0.5 * dt)
+        self.time += dt
+        self.steps += 1
+        if self.interval > 0 and self.steps % self.interval == 0:
+            self.regrid()
 
-    def totals(self):
-        """Conserved totals over the leaf cells of both levels (per unit depth)."""
+    def regrid(self):
+        before, scale = self.totals(), self.totals(absolute=True)
+        c = oracle.fill_ghosts(self.g0, self.X[0].copy())
+        tags, st = oracle.tag(self.g0, c, self.time, self.crit)
+        if st:
+            raise RuntimeError("ErrorEst: inadmissible level-0 cell")
+        B, h, buf = self.B, self.B // 2, self.buf
+        nby, nbx = self.active.shape
+        nxt = np.zeros_like(self.active)
+        for bj in range(nby):
+            for bi in range(nbx):
+                rows = np.arange(bj * h - buf, (bj + 1) * h + buf) % self.ny
+                cols = np.arange(bi * h - buf, (bi + 1) * h + buf) % self.nx
+                nxt[bj, bi] = 1 if tags[np.ix_(rows, cols)].any() else 0
+        f = self.X[1]
+        for bj, bi in zip(*np.nonzero(nxt & (1 - self.active))):
+            for fj in range(bj * B, (bj + 1) * B):
+                for fi in range(bi * B, (bi + 1) * B):
+                    ci, cj = fi >> 1, fj >> 1
+                    kids, _ = oracle.interp_cell(c[cj + 2, ci + 2], c[cj + 2, ci + 1], c[cj + 2, ci + 3],
+                                                 c[cj + 1, ci + 2], c[cj + 3, ci + 2])
+                    f[fj + 2, fi + 2] = kids[(fj & 1) * 2 + (fi & 1)]
+        self.active = nxt
+        self.blocks = [(bi, bj) for bj in range(nby) for bi in range(nbx) if self.active[bj, bi]]
+        self.regions = self._regions()
+        self.regrids += 1
+        after = self.totals()
+        if np.any(np.abs(after - before) > 1e-8 * scale):
+            raise RuntimeError("regridChecked: the totals changed in the remap")
+
+    def totals(self, absolute=False):
+        """Conserved totals over the leaf cells of both levels (per unit depth); absolute:
+        of the magnitudes."""
         B = self.B
         v0, v1 = self.dx * self.dy, self.dx * self.dy / 4
-        t = self.X[0][2:-2, 2:-2][self.leaf_mask0()].sum(0) * v0
+        a = np.abs if absolute else (lambda x: x)
+        t = a(self.X[0][2:-2, 2:-2][self.leaf_mask0()]).sum(0) * v0
         for bi, bj in self.blocks:
-            t = t + self.X[1][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B].reshape(-1, self.nv).sum(0) * v1
+            t = t + a(self.X[1][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B]).reshape(-1, self.nv).sum(0) * v1
         return t
 
     def level(self, l):
