@@ -67,3 +67,29 @@ def test_init_rejects_unknown_mechanism(lib):
     h = ctypes.c_void_p()
     assert lib.hf_init(b"gri30.yaml", 0, ctypes.byref(h)) == 4  # HF_ERR_ARG, before touching a device
     assert not h.value
+
+
+def test_every_struct_mirror_matches_header(tmp_path):
+    """Every ctypes mirror of a header struct: sizeof and the offset of every named field
+    as the C compiler lays them out."""
+    import subprocess
+    from hyperflow_gb300 import _lib
+    mirrors = {"hf_level": _lib.Level, "hf_patch": _lib.Patch, "hf_counters": _lib.Counters,
+               "hf_chem_history": _lib.ChemHistory, "hf_adjoint_opts": _lib.AdjointOpts,
+               "hf_tag_criteria": _lib.TagCriteria, "hf_amr_opts": _lib.AmrOpts}
+    lines, want = [], []
+    for cname, py in mirrors.items():
+        lines.append('  printf("%%zu\\n", sizeof(%s));' % cname)
+        want.append(ctypes.sizeof(py))
+        for f in py._fields_:
+            if f[0].startswith("pad"):
+                continue
+            lines.append('  printf("%%zu\\n", offsetof(%s, %s));' % (cname, f[0]))
+            want.append(getattr(py, f[0]).offset)
+    src = tmp_path / "layouts.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"hyperflow_gpu.h\"\nint main(void) {\n" +
+                   "\n".join(lines) + "\n  return 0;\n}\n")
+    exe = tmp_path / "layouts"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
