@@ -243,3 +243,35 @@ def test_amr_regrid_run_matches_composite_oracle(gpu, oracle):
     for got, ref in pairs:
         assert np.max(np.abs(got - ref) / scale) < 1e-10
     m.close()
+
+
+def test_run_amr_case_writes_reference_files(gpu, tmp_path):
+    """BlockAMR::run on three levels through run_amr_case: the reference's files at t = 0
+    and two output times, each state file a tiling of the domain by leaf cells
+    (validate.py:64-78), mass and energy conserved on the periodic box to 1e-11
+    (validate.py:133), one history row per step."""
+    import json
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import output, workloads as W
+    from test_output_amr import check_geometry
+    U, lvd = W.det2d(seed=6, diluent="N2", nx=32, ny=16, hot_columns=6)
+    lvd = dict(lvd, periodic=(1, 1))
+    lv = hf.make_level(**lvd)
+    s = output.run_amr_case(gpu, lv, cuda(U), 2e-8, str(tmp_path), cfl=0.5, output_times=[1e-8, 2e-8], max_level=2,
+                            block=16, tag_buffer=1, regrid_interval=2, chem="batched",
+                            tags=dict(pressure_tag=0.08, temperature_tag=0.08, density_tag=0.05))
+    names = sorted(os.listdir(tmp_path))
+    assert names == ["boxes_0.csv", "boxes_1.csv", "boxes_2.csv", "history.csv", "state_0.csv", "state_1.csv",
+                     "state_2.csv", "summary.json"]
+    assert s["completed"] and s["final_time"] == 2e-8 and s["retries"] == 0 and s["finest_level"] >= 1
+    for k in range(3):
+        data = np.genfromtxt(tmp_path / ("state_%d.csv" % k), names=True, delimiter=",")
+        check_geometry(data, (32, 16), (32 * lvd["dx"], 16 * lvd["dy"]), int(data["level"].max()))
+        Y = np.column_stack([data[n] for n in data.dtype.names if n.startswith("Y_")])
+        assert np.min(Y) >= 0 and np.max(np.abs(Y.sum(1) - 1)) < 1e-12
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+    hist = np.genfromtxt(tmp_path / "history.csv", names=True, delimiter=",")
+    assert len(hist) == s["steps"] + 1 and hist["regrids"][-1] == s["regrids"]
+    assert np.all(hist["leaf_cells"] > 0)
