@@ -3,31 +3,40 @@ import it; the GPU package never does.
 
 A restatement, with the oracle's per-cell functions, of the multi-level stepper's
 algorithm at refinement ratio 2 without time subcycling (HyperFlow_V3/src/BlockAMR.cpp:
-euler :202-264, flow :266-270, react :271-285, regrid :367-373 with ErrorEst :170-200).
-Scope: two levels, periodic in x and y.
-- Ghosts: level 0 by the periodic fill; level 1 by the periodic images of its dense
-  array, then, in each active block's 2-cell frame part that lies in an inactive block
-  (across a periodic edge: the inactive periodic image), ConservativeInterp from level 0
+euler :202-264, flow :266-270, react :271-285, regrid :367-373 with ErrorEst :170-200),
+on levels 0..max_level of a domain with the reference's boundary conditions.
+- Level l is a dense ghosted array over the whole domain refined 2^l times; level 0 is
+  always fully active, level l >= 1 is active in aligned blocks of `block` cells.
+- Ghosts: every level by the physical/periodic fill of its whole array, then, in each
+  active block's 2-cell frame part that lies in an inactive block of the same level
+  (across a periodic edge: the inactive periodic image; outside a non-periodic edge:
+  none, the physical ghosts stay), ConservativeInterp from level l-1
   (src/ConservativeInterp.cpp:18-51, oracle.interp_cell).
-- Euler stage: level 0 as one periodic box, level 1 block by block (no wall faces inside
-  the periodic domain), then reflux of level 0 from the fine face fluxes
-  (FluxRegister, :245-256) and average_down (:256).
+- Euler stage: level 0 as one box, level l >= 1 block by block (a block face is a wall
+  face only where it lies on a reflecting or wedge domain edge), then from the finest
+  level down: reflux of level l-1 from level l's face fluxes (FluxRegister, :245-256)
+  and average_down (:256).  Not restated: the first-order redo and the roundoff repair
+  (an inadmissible stage or a negative species raises; the cases compared never need
+  them).
 - flow(h): two stages, Heun combination, average_down, validation.
-- react(dt): the leaf cells of both levels (level-0 cells under no active block, every
-  active level-1 cell) through the oracle's ChemistryBatch, then average_down.
-- regrid (every regrid_interval steps, and once to build the initial hierarchy from the
-  base level alone): ErrorEst tags of level 0; a level-1 block is active when a tagged
-  cell lies in its level-0 footprint grown by tag_buffer cells (wrapping across the
-  periodic edges; proper nesting always holds under a fully active level 0).  Blocks
-  that become active are filled by ConservativeInterp from level 0; blocks that stay
-  keep their data; nothing is averaged.  The leaf totals must survive the remap to 1e-8
-  of the total of the magnitudes (regridChecked, :369-371).  The block rule is the GPU
-  stepper's deterministic choice in place of AMReX's clustering.
+- react(dt): the leaf cells of every level through the oracle's ChemistryBatch, then
+  average_down.
+- regrid (every regrid_interval steps, and max_level times to build the initial
+  hierarchy from the base level alone), level by level from 0: ErrorEst tags of level
+  l's active cells; a level-(l+1) block is active when a tagged cell lies in its level-l
+  footprint grown by tag_buffer cells and the footprint grown by 2 cells lies in active
+  level-l cells (proper nesting); both wrap across periodic edges and are cut at the
+  others.  Blocks that become active are filled by ConservativeInterp from level l;
+  blocks that stay keep their data; nothing is averaged.  The leaf totals must survive
+  the remap to 1e-8 of the total of the magnitudes (regridChecked, :369-371).  The block
+  rule is the GPU stepper's deterministic choice in place of AMReX's clustering.
 States are AoS arrays (..., NS+3); levels are dense ghosted arrays (ny+4, nx+4, NV).
 """
 import numpy as np
 
 import oracle
+
+BC = {"reflecting": 0, "transmissive": 1, "inflow": 2, "wedge": 3}
 
 
 def criteria(pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, density_tag=0.0, chemistry=True,
@@ -44,161 +53,234 @@ def criteria(pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, densit
     return c
 
 
-class AmrOracle:
-    def __init__(self, U0, U1, active, dx, dy, block, chemistry=True, rtol=1e-8, atol=1e-15, crit=None,
-                 tag_buffer=1, regrid_interval=0):
-        """U0: (ny, nx, NV) level 0; U1: (2ny, 2nx, NV) level 1 (read in active blocks);
-        active: (nby, nbx) uint8 of level-1 blocks (block x block fine cells); crit:
-        criteria(...) for regrids."""
-        ny, nx, nv = U0.shape
-        if U1.shape != (2 * ny, 2 * nx, nv):
-            raise ValueError("level 1 must be the level-0 domain at ratio 2")
-        self.nx, self.ny, self.nv, self.B = nx, ny, nv, block
-        self.dx, self.dy = dx, dy
-        self.active = np.asarray(active, dtype=np.uint8)
-        nby, nbx = self.active.shape
-        if nbx * block != 2 * nx or nby * block != 2 * ny:
-            raise ValueError("blocks must tile level 1")
-        self.blocks = [(bi, bj) for bj in range(nby) for bi in range(nbx) if self.active[bj, bi]]
+def _wrap(n, count, periodic):
+    """Index n along a direction of `count`: wrapped when periodic, -1 outside."""
+    if 0 <= n < count:
+        return n
+    return n % count if periodic else -1
+
+
+class Hierarchy:
+    def __init__(self, Us, actives, domain, block, chemistry=True, rtol=1e-8, atol=1e-15, crit=None,
+                 tag_buffer=1, regrid_interval=0, max_level=None):
+        """Us[l]: (ny_l, nx_l, NV) state of level l (read in its active blocks); actives[l]:
+        (nby_l, nbx_l) uint8 for l >= 1 (actives[0] is ignored: level 0 is all active);
+        domain: the base level's keys (nx, ny, dx, dy, xlo, ylo, periodic, boundary_lo,
+        boundary_hi, inlet, wedge_start); crit: criteria(...) for regrids."""
+        d = dict(xlo=0.0, ylo=0.0, periodic=(1, 1), boundary_lo=("reflecting", "reflecting"),
+                 boundary_hi=("transmissive", "reflecting"), inlet=None, wedge_start=0.0)
+        d.update(domain)
+        self.d = d
+        nx, ny = d["nx"], d["ny"]
+        self.nv, self.B = Us[0].shape[2], block
+        self.max_level = len(Us) - 1 if max_level is None else max_level
+        L = self.max_level + 1
+        if block % 2 or (L > 1 and (nx % (block // 2) or ny % (block // 2))):
+            raise ValueError("blocks must tile the refined levels")
+        self.px, self.py = int(d["periodic"][0]), int(d["periodic"][1])
+        self.inlet = np.zeros(self.nv) if d["inlet"] is None else np.asarray(d["inlet"], dtype=np.float64)
+        self.shape = [(ny << l, nx << l) for l in range(L)]
+        self.dxs = [(d["dx"] / (1 << l), d["dy"] / (1 << l)) for l in range(L)]
+        self.g = [self._grid(l, 0, 0, *self.shape[l][::-1]) for l in range(L)]
+        self.nb = [((self.shape[l][0] + block - 1) // block, (self.shape[l][1] + block - 1) // block)
+                   for l in range(L)]
+        self.X = []
+        self.acts = [np.ones(self.nb[0], np.uint8)]
+        for l in range(L):
+            U = np.zeros(self.shape[l] + (self.nv,)) if l >= len(Us) else np.asarray(Us[l], dtype=np.float64)
+            if U.shape != self.shape[l] + (self.nv,):
+                raise ValueError("level %d has shape %s, expected %s" % (l, U.shape, self.shape[l]))
+            self.X.append(oracle.ghosted(U))
+            if l:
+                a = actives[l] if l < len(actives) and actives[l] is not None else np.zeros(self.nb[l], np.uint8)
+                self.acts.append(np.asarray(a, dtype=np.uint8).copy())
+        self.finest = 0
+        for l in range(1, L):
+            if self.acts[l].any():
+                self.finest = l
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
         self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
         self.time, self.steps, self.regrids = 0.0, 0, 0
-        self.g0 = oracle.make_grid(nx, ny, dx, dy, periodic=(1, 1))
-        self.g1 = oracle.make_grid(2 * nx, 2 * ny, dx / 2, dy / 2, periodic=(1, 1))
-        # one block as its own box: transmissive sides (no wall faces in a periodic domain)
-        self.gb = oracle.make_grid(block, block, dx / 2, dy / 2, periodic=(0, 0), bc_lo=(1, 1), bc_hi=(1, 1))
-        self.X = [oracle.ghosted(np.array(U0, dtype=np.float64)), oracle.ghosted(np.array(U1, dtype=np.float64))]
-        self.regions = self._regions()
-        self.X[0][2:-2, 2:-2] = self._averaged(self.X[1], self.X[0])[2:-2, 2:-2]
+        self._rebuild()
+        self.X = self.average_all(self.X)
 
     @classmethod
-    def from_base(cls, U0, dx, dy, block, crit, tag_buffer=1, regrid_interval=0, **kw):
-        """The hierarchy the GPU stepper builds from the base level alone: level 0 = U0,
-        then one regrid (hf_amr_create)."""
-        ny, nx, nv = U0.shape
-        o = cls(U0, np.zeros((2 * ny, 2 * nx, nv)), np.zeros((2 * ny // block, 2 * nx // block), np.uint8), dx, dy,
-                block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval, **kw)
-        o.regrid()
+    def from_base(cls, U0, domain, block, crit, max_level=1, tag_buffer=1, regrid_interval=0, **kw):
+        """The hierarchy the GPU stepper builds from the base level alone (hf_amr_create):
+        level 0 = U0, then one regrid per level."""
+        o = cls([U0], [None], domain, block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval,
+                max_level=max_level, **kw)
+        for _ in range(max_level):
+            o.regrid()
         o.regrids = 0
         return o
 
-    # ------------------------------------------------------------ hierarchy
-    def _regions(self):
-        """Coarse-fine regions (i0, j0, i1, j1) in level-1 indices."""
-        B, (nby, nbx) = self.B, self.active.shape
-        out = []
-        for bi, bj in self.blocks:
-            ilo, jlo = bi * B, bj * B
-            for dj in (-1, 0, 1):
-                for di in (-1, 0, 1):
-                    if not di and not dj:
-                        continue
-                    if self.active[(bj + dj) % nby, (bi + di) % nbx]:
-                        continue
-                    i0 = ilo - 2 if di < 0 else (ilo + B if di > 0 else ilo)
-                    i1 = ilo - 1 if di < 0 else (ilo + B + 1 if di > 0 else ilo + B - 1)
-                    j0 = jlo - 2 if dj < 0 else (jlo + B if dj > 0 else jlo)
-                    j1 = jlo - 1 if dj < 0 else (jlo + B + 1 if dj > 0 else jlo + B - 1)
-                    out.append((i0, j0, i1, j1))
-        return out
+    # ------------------------------------------------------------ geometry
+    def _grid(self, l, i0, j0, nx, ny):
+        """Grid of level l's box of nx x ny cells from cell (i0, j0): the domain's
+        conditions on the sides that lie on a non-periodic domain edge, transmissive
+        (no wall face) elsewhere."""
+        d, (NY, NX) = self.d, self.shape[l]
+        lo = [BC[d["boundary_lo"][0]], BC[d["boundary_lo"][1]]]
+        hi = [BC[d["boundary_hi"][0]], BC[d["boundary_hi"][1]]]
+        whole = (i0, j0, nx, ny) == (0, 0, NX, NY)
+        if not whole:
+            lo[0] = lo[0] if i0 == 0 and not self.px else BC["transmissive"]
+            hi[0] = hi[0] if i0 + nx == NX and not self.px else BC["transmissive"]
+            lo[1] = lo[1] if j0 == 0 and not self.py else BC["transmissive"]
+            hi[1] = hi[1] if j0 + ny == NY and not self.py else BC["transmissive"]
+        dx, dy = self.dxs[l]
+        return oracle.make_grid(nx, ny, dx, dy, xlo=d["xlo"] + i0 * dx, ylo=d["ylo"] + j0 * dy,
+                                periodic=(self.px, self.py) if whole else (0, 0), bc_lo=tuple(lo), bc_hi=tuple(hi),
+                                inlet=self.inlet, wedge_start=d["wedge_start"])
 
-    def leaf_mask0(self):
-        """(ny, nx) True where a level-0 cell lies under no active level-1 block."""
-        cov = np.kron(self.active, np.ones((self.B // 2, self.B // 2), dtype=np.uint8)).astype(bool)
-        return ~cov
+    def blocks(self, l):
+        """Active blocks (bi, bj) of level l >= 1, row-major."""
+        nby, nbx = self.nb[l]
+        return [(bi, bj) for bj in range(nby) for bi in range(nbx) if self.acts[l][bj, bi]]
+
+    def _rebuild(self):
+        self.regions = [[] for _ in range(self.max_level + 1)]
+        B = self.B
+        for l in range(1, self.finest + 1):
+            nby, nbx = self.nb[l]
+            for bi, bj in self.blocks(l):
+                ilo, jlo = bi * B, bj * B
+                for dj in (-1, 0, 1):
+                    for di in (-1, 0, 1):
+                        if not di and not dj:
+                            continue
+                        nbi, nbj = _wrap(bi + di, nbx, self.px), _wrap(bj + dj, nby, self.py)
+                        if nbi < 0 or nbj < 0 or self.acts[l][nbj, nbi]:
+                            continue
+                        i0 = ilo - 2 if di < 0 else (ilo + B if di > 0 else ilo)
+                        i1 = ilo - 1 if di < 0 else (ilo + B + 1 if di > 0 else ilo + B - 1)
+                        j0 = jlo - 2 if dj < 0 else (jlo + B if dj > 0 else jlo)
+                        j1 = jlo - 1 if dj < 0 else (jlo + B + 1 if dj > 0 else jlo + B - 1)
+                        self.regions[l].append((i0, j0, i1, j1))
+
+    def leaf_mask(self, l):
+        """(ny_l, nx_l) True at the leaf cells of level l."""
+        ny, nx = self.shape[l]
+        B, h = self.B, self.B // 2
+        m = np.ones((ny, nx), bool) if l == 0 else np.kron(self.acts[l], np.ones((B, B), np.uint8)).astype(bool)[
+            :ny, :nx]
+        if l < self.finest:
+            m &= ~np.kron(self.acts[l + 1], np.ones((h, h), np.uint8)).astype(bool)[:ny, :nx]
+        return m
+
+    # ------------------------------------------------------------ hierarchy operations
+    def _interp(self, f, c, fj, fi):
+        """ConservativeInterp child of fine cell (fi, fj) from the ghosted coarse array c."""
+        ci, cj = fi >> 1, fj >> 1
+        kids, _ = oracle.interp_cell(c[cj + 2, ci + 2], c[cj + 2, ci + 1], c[cj + 2, ci + 3], c[cj + 1, ci + 2],
+                                     c[cj + 3, ci + 2])
+        f[fj + 2, fi + 2] = kids[(fj & 1) * 2 + (fi & 1)]
 
     def fill(self, X):
-        X[0] = oracle.fill_ghosts(self.g0, X[0])
-        f = X[1]
-        inner = f[2:-2, 2:-2]
-        f[:] = np.pad(inner, ((2, 2), (2, 2), (0, 0)), mode="wrap")
-        c = X[0]
-        for i0, j0, i1, j1 in self.regions:
-            for fj in range(j0, j1 + 1):
-                for fi in range(i0, i1 + 1):
-                    ci, cj = fi >> 1, fj >> 1
-                    q = c[cj + 2, ci + 2]
-                    kids, _ = oracle.interp_cell(q, c[cj + 2, ci + 1], c[cj + 2, ci + 3], c[cj + 1, ci + 2],
-                                                 c[cj + 3, ci + 2])
-                    f[fj + 2, fi + 2] = kids[(fj & 1) * 2 + (fi & 1)]
+        """Ghosts of every level (coarse levels first)."""
+        for l in range(self.finest + 1):
+            X[l] = oracle.fill_ghosts(self.g[l], X[l])
+            for i0, j0, i1, j1 in self.regions[l]:
+                for fj in range(j0, j1 + 1):
+                    for fi in range(i0, i1 + 1):
+                        self._interp(X[l], X[l - 1], fj, fi)
         return X
 
-    def _averaged(self, fine, coarse):
-        """coarse with every active block's footprint replaced by the average of its children."""
+    def _averaged(self, l, fine, coarse):
+        """coarse with every active level-l block's footprint replaced by the average of
+        its children."""
         out = coarse.copy()
         B, h = self.B, self.B // 2
-        for bi, bj in self.blocks:
+        for bi, bj in self.blocks(l):
             avg = oracle.average_down(fine[2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B])
             out[2 + bj * h:2 + (bj + 1) * h, 2 + bi * h:2 + (bi + 1) * h] = avg
         return out
 
+    def average_all(self, X):
+        X = list(X)
+        for l in range(self.finest, 0, -1):
+            X[l - 1] = self._averaged(l, X[l], X[l - 1])
+        return X
+
+    def _active_cells(self, X, l):
+        cells = X[l][2:-2, 2:-2]
+        if l == 0:
+            return cells.reshape(-1, self.nv)
+        B = self.B
+        return np.concatenate([cells[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, self.nv)
+                               for bi, bj in self.blocks(l)])
+
     def _check(self, X, what):
-        for l in range(2):
-            cells = X[l][2:-2, 2:-2]
-            if l == 1:
-                B = self.B
-                cells = np.concatenate([cells[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, self.nv)
-                                        for bi, bj in self.blocks]) if self.blocks else cells[:0].reshape(-1, self.nv)
-            st = oracle.properties(cells.reshape(-1, self.nv))[3]
-            if np.any(st):
+        for l in range(self.finest + 1):
+            if np.any(oracle.properties(self._active_cells(X, l))[3]):
                 raise RuntimeError("inadmissible level-%d cell after %s" % (l, what))
 
-    # ------------------------------------------------------------ step
     def euler(self, Xin, h):
         Xin = self.fill([x.copy() for x in Xin])
         out = [x.copy() for x in Xin]
-        o0, fx0, fy0, st = oracle.euler_stage(self.g0, Xin[0], h)
-        if st:
-            raise RuntimeError("level-0 face inadmissible")
-        out[0][2:-2, 2:-2] = o0[2:-2, 2:-2]
         B = self.B
-        boxes, fxl, fyl = [], [], []
-        for bi, bj in self.blocks:
-            i0, j0 = bi * B, bj * B
-            ob, fxb, fyb, st = oracle.euler_stage(self.gb, Xin[1][j0:j0 + B + 4, i0:i0 + B + 4], h)
-            if st:
-                raise RuntimeError("level-1 face inadmissible")
-            out[1][j0 + 2:j0 + 2 + B, i0 + 2:i0 + 2 + B] = ob[2:-2, 2:-2]
-            boxes.append((i0, j0, i0 + B - 1, j0 + B - 1))
-            fxl.append(fxb)
-            fyl.append(fyb)
+        FX, FY, fine = [], [], []
+        for l in range(self.finest + 1):
+            ny, nx = self.shape[l]
+            if l == 0:
+                o, fx, fy, st = oracle.euler_stage(self.g[0], Xin[0], h)
+                if st:
+                    raise RuntimeError("level-0 face inadmissible")
+                out[0][2:-2, 2:-2] = o[2:-2, 2:-2]
+                FX.append(fx)
+                FY.append(fy)
+                fine.append(None)
+                continue
+            fxa, fya = np.zeros((ny, nx + 1, self.nv)), np.zeros((ny + 1, nx, self.nv))
+            boxes, fxl, fyl = [], [], []
+            for bi, bj in self.blocks(l):
+                i0, j0 = bi * B, bj * B
+                o, fx, fy, st = oracle.euler_stage(self._grid(l, i0, j0, B, B), Xin[l][j0:j0 + B + 4, i0:i0 + B + 4], h)
+                if st:
+                    raise RuntimeError("level-%d face inadmissible" % l)
+                out[l][j0 + 2:j0 + 2 + B, i0 + 2:i0 + 2 + B] = o[2:-2, 2:-2]
+                fxa[j0:j0 + B, i0:i0 + B + 1] = fx
+                fya[j0:j0 + B + 1, i0:i0 + B] = fy
+                boxes.append((i0, j0, i0 + B - 1, j0 + B - 1))
+                fxl.append(fx)
+                fyl.append(fy)
+            FX.append(fxa)
+            FY.append(fya)
+            fine.append((boxes, fxl, fyl))
         self._check(out, "a stage")
-        if boxes:
-            out[0][2:-2, 2:-2] = oracle.reflux(out[0][2:-2, 2:-2], fx0, fy0, boxes, fxl, fyl, h, self.dx, self.dy,
-                                               periodic=(1, 1))
-        out[0] = self._averaged(out[1], out[0])
+        for l in range(self.finest, 0, -1):
+            boxes, fxl, fyl = fine[l]
+            dx, dy = self.dxs[l - 1]
+            out[l - 1][2:-2, 2:-2] = oracle.reflux(out[l - 1][2:-2, 2:-2], FX[l - 1], FY[l - 1], boxes, fxl, fyl, h, dx,
+                                                   dy, periodic=(self.px, self.py))
+            out[l - 1] = self._averaged(l, out[l], out[l - 1])
         return out
 
     def flow(self, h):
         U = self.X
         S = self.euler(U, h)
         N = self.euler(S, h)
-        for l in range(2):
+        for l in range(len(N)):
             N[l] = 0.5 * U[l] + 0.5 * N[l]
-        N[0] = self._averaged(N[1], N[0])
+        N = self.average_all(N)
         self._check(N, "the Heun combination")
         self.X = N
 
     def react(self, dt):
         if not self.chemistry:
             return
-        B, nv = self.B, self.nv
-        m0 = self.leaf_mask0()
-        c0 = self.X[0][2:-2, 2:-2]
-        cells = [c0[m0]]
-        for bi, bj in self.blocks:
-            cells.append(self.X[1][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B].reshape(-1, nv))
-        batch = np.concatenate(cells)
+        masks = [self.leaf_mask(l) for l in range(self.finest + 1)]
+        batch = np.concatenate([self.X[l][2:-2, 2:-2][masks[l]] for l in range(self.finest + 1)])
         out, bad, _ = oracle.chem_batch(batch, dt, rtol=self.rtol, atol=self.atol)
         if bad >= 0:
             raise RuntimeError("chemistry cell %d failed" % bad)
-        n0 = int(m0.sum())
-        c0[m0] = out[:n0]
-        k = n0
-        for bi, bj in self.blocks:
-            self.X[1][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B] = out[k:k + B * B].reshape(B, B, nv)
-            k += B * B
-        self.X[0] = self._averaged(self.X[1], self.X[0])
+        k = 0
+        for l in range(self.finest + 1):
+            n = int(masks[l].sum())
+            self.X[l][2:-2, 2:-2][masks[l]] = out[k:k + n]
+            k += n
+        self.X = self.average_all(self.X)
         self._check(self.X, "react")
 
     def step(self, dt):
@@ -210,46 +292,111 @@ class AmrOracle:
         if self.interval > 0 and self.steps % self.interval == 0:
             self.regrid()
 
-    def regrid(self):
-        before, scale = self.totals(), self.totals(absolute=True)
-        c = oracle.fill_ghosts(self.g0, self.X[0].copy())
-        tags, st = oracle.tag(self.g0, c, self.time, self.crit)
-        if st:
-            raise RuntimeError("ErrorEst: inadmissible level-0 cell")
+    # ------------------------------------------------------------ regrid
+    def _regrid_level(self, l):
         B, h, buf = self.B, self.B // 2, self.buf
-        nby, nbx = self.active.shape
-        nxt = np.zeros_like(self.active)
+        self.X = self.fill(self.X)
+        c = self.X[l]
+        ny, nx = self.shape[l]
+        # ErrorEst on the active cells of level l (level 0 as one box, blocks one by one)
+        if l == 0:
+            tags, st = oracle.tag(self.g[0], c, self.time, self.crit)
+            if st:
+                raise RuntimeError("ErrorEst: inadmissible level-0 cell")
+            tags = tags.astype(bool)
+        else:
+            tags = np.zeros((ny, nx), bool)
+            for bi, bj in self.blocks(l):
+                i0, j0 = bi * B, bj * B
+                t, st = oracle.tag(self._grid(l, i0, j0, B, B), c[j0:j0 + B + 4, i0:i0 + B + 4], self.time, self.crit)
+                if st:
+                    raise RuntimeError("ErrorEst: inadmissible level-%d cell" % l)
+                tags[j0:j0 + B, i0:i0 + B] = t.astype(bool)
+        act = np.ones((ny, nx), bool) if l == 0 else np.kron(self.acts[l], np.ones((B, B), np.uint8)).astype(bool)[
+            :ny, :nx]
+        nby, nbx = self.nb[l + 1]
+
+        def cells(lo, n, count, periodic):
+            idx = [_wrap(k, count, periodic) for k in range(lo, lo + n)]
+            return np.array([k for k in idx if k >= 0], dtype=np.int64)
+
+        nxt = np.zeros((nby, nbx), np.uint8)
         for bj in range(nby):
             for bi in range(nbx):
-                rows = np.arange(bj * h - buf, (bj + 1) * h + buf) % self.ny
-                cols = np.arange(bi * h - buf, (bi + 1) * h + buf) % self.nx
-                nxt[bj, bi] = 1 if tags[np.ix_(rows, cols)].any() else 0
-        f = self.X[1]
-        for bj, bi in zip(*np.nonzero(nxt & (1 - self.active))):
+                i0, j0 = bi * h, bj * h
+                iw, jw = min(i0 + h, nx) - i0, min(j0 + h, ny) - j0
+                rows, cols = cells(j0 - buf, jw + 2 * buf, ny, self.py), cells(i0 - buf, iw + 2 * buf, nx, self.px)
+                if not tags[np.ix_(rows, cols)].any():
+                    continue
+                rows, cols = cells(j0 - 2, jw + 4, ny, self.py), cells(i0 - 2, iw + 4, nx, self.px)
+                nxt[bj, bi] = 1 if act[np.ix_(rows, cols)].all() else 0
+        prev, had = self.acts[l + 1], self.finest >= l + 1
+        self.acts[l + 1] = nxt
+        anyb = bool(nxt.any())
+        self.finest = max(self.finest, l + 1) if anyb else l
+        f = self.X[l + 1]
+        for bj, bi in zip(*np.nonzero(nxt)):
+            if had and prev[bj, bi]:
+                continue
             for fj in range(bj * B, (bj + 1) * B):
                 for fi in range(bi * B, (bi + 1) * B):
-                    ci, cj = fi >> 1, fj >> 1
-                    kids, _ = oracle.interp_cell(c[cj + 2, ci + 2], c[cj + 2, ci + 1], c[cj + 2, ci + 3],
-                                                 c[cj + 1, ci + 2], c[cj + 3, ci + 2])
-                    f[fj + 2, fi + 2] = kids[(fj & 1) * 2 + (fi & 1)]
-        self.active = nxt
-        self.blocks = [(bi, bj) for bj in range(nby) for bi in range(nbx) if self.active[bj, bi]]
-        self.regions = self._regions()
+                    self._interp(f, c, fj, fi)
+        if not anyb:
+            for q in range(l + 2, self.max_level + 1):
+                self.acts[q][:] = 0
+        self._rebuild()
+
+    def regrid(self):
+        before, scale = self.totals(), self.totals(absolute=True)
+        l = 0
+        while l < self.max_level and l <= self.finest:
+            self._regrid_level(l)
+            l += 1
         self.regrids += 1
         after = self.totals()
         if np.any(np.abs(after - before) > 1e-8 * scale):
             raise RuntimeError("regridChecked: the totals changed in the remap")
 
+    # ------------------------------------------------------------ results
     def totals(self, absolute=False):
-        """Conserved totals over the leaf cells of both levels (per unit depth); absolute:
+        """Conserved totals over the leaf cells of every level (per unit depth); absolute:
         of the magnitudes."""
-        B = self.B
-        v0, v1 = self.dx * self.dy, self.dx * self.dy / 4
         a = np.abs if absolute else (lambda x: x)
-        t = a(self.X[0][2:-2, 2:-2][self.leaf_mask0()]).sum(0) * v0
-        for bi, bj in self.blocks:
-            t = t + a(self.X[1][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B]).reshape(-1, self.nv).sum(0) * v1
+        t = np.zeros(self.nv)
+        for l in range(self.finest + 1):
+            dx, dy = self.dxs[l]
+            t = t + a(self.X[l][2:-2, 2:-2][self.leaf_mask(l)]).sum(0) * (dx * dy)
         return t
 
     def level(self, l):
         return self.X[l][2:-2, 2:-2].copy()
+
+
+class AmrOracle(Hierarchy):
+    """Two levels of a domain periodic in x and y (origin 0): U0 (ny, nx, NV), U1
+    (2ny, 2nx, NV) read in the active blocks, active (nby, nbx) of level 1."""
+
+    def __init__(self, U0, U1, active, dx, dy, block, **kw):
+        ny, nx, nv = np.shape(U0)
+        if np.shape(U1) != (2 * ny, 2 * nx, nv):
+            raise ValueError("level 1 must be the level-0 domain at ratio 2")
+        if np.shape(active) != (2 * ny // block, 2 * nx // block):
+            raise ValueError("blocks must tile level 1")
+        super().__init__([U0, U1], [None, active], dict(nx=nx, ny=ny, dx=dx, dy=dy, periodic=(1, 1)), block, **kw)
+
+    @classmethod
+    def from_base(cls, U0, dx, dy, block, crit, tag_buffer=1, regrid_interval=0, **kw):
+        ny, nx, nv = np.shape(U0)
+        o = cls(U0, np.zeros((2 * ny, 2 * nx, nv)), np.zeros((2 * ny // block, 2 * nx // block), np.uint8), dx, dy,
+                block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval, **kw)
+        o.regrid()
+        o.regrids = 0
+        return o
+
+    @property
+    def active(self):
+        """(nby, nbx) uint8 active blocks of level 1."""
+        return self.acts[1]
+
+    def leaf_mask0(self):
+        return self.leaf_mask(0)

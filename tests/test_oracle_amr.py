@@ -1,7 +1,9 @@
 """The CPU oracle of the block-AMR composite step (oracle/amr.py) on its own: with every
-level-1 block active it is the one-level run of the fine grid bit for bit, with none it
-is the one-level run of the coarse grid, and with part of level 1 active it conserves
-mass, momentum and energy over the leaf cells (reflux and average_down)."""
+block active it is the one-level run of the finest grid bit for bit (periodic, walled
+and wedge/inflow domains, two and three levels), with none it is the one-level run of
+the coarse grid, and with part of the hierarchy active it conserves mass, momentum and
+energy over the leaf cells (reflux and average_down); regrids follow the tags, nest the
+levels and conserve."""
 import numpy as np
 import pytest
 
@@ -119,4 +121,105 @@ def test_regrid_twice_changes_nothing(oracle, amr_oracle):
     a = amr_oracle.AmrOracle.from_base(U0, dx, dx, B, crit, tag_buffer=2, chemistry=False)
     act, l0, l1 = a.active.copy(), a.level(0), a.level(1)
     a.regrid()
-    assert np.array_equal(a.active, act) and np.array_equal(a.level(0), l0) and np.array_equal(a.level(1), l1)
+    # (cells of inactive blocks hold ghost-frame values of the fill, not state)
+    m = np.kron(act, np.ones((B, B), np.uint8)).astype(bool)
+    assert np.array_equal(a.active, act) and np.array_equal(a.level(0), l0) and np.array_equal(a.level(1)[m], l1[m])
+
+
+def _grid_run(oracle, g, U, dt, nsteps):
+    Ug = oracle.fill_ghosts(g, oracle.ghosted(U))
+    for _ in range(nsteps):
+        Ug, dta, st, _ = oracle.strang_step(g, Ug, dt)
+        assert st == 0 and dta == dt
+    return Ug[2:-2, 2:-2]
+
+
+def _coarsen(F, times):
+    for _ in range(times):
+        F = (((F[0::2, 0::2] + F[0::2, 1::2]) + F[1::2, 0::2]) + F[1::2, 1::2]) * 0.25
+    return F
+
+
+@pytest.mark.parametrize("case", ["periodic", "walls", "wedge"])
+def test_three_levels_fully_refined_are_the_finest_run(oracle, amr_oracle, case):
+    """Every level-1 and level-2 block active: level 2 is the one-level run of the finest
+    grid bit for bit; the wall and wedge cases check that a block face is a wall face
+    exactly where it lies on the domain's wall."""
+    from hyperflow_gb300 import workloads as W
+    nx, ny, B = 8, 4, 8
+    if case == "wedge":
+        _, lvd = W.wedge(nx=nx, ny=ny, length=0.004, x_tip=0.001)
+        U2 = np.tile(lvd["inlet"], (4 * ny, 4 * nx, 1))
+        U2 *= (1.0 + 0.05 * np.sin(np.arange(4 * nx) / 3.0))[None, :, None]  # density waves
+        dx = lvd["dx"]
+    else:
+        dx = 1e-4
+        U2 = H.smooth_field(4 * nx, 4 * ny, seed=11)
+        lvd = dict(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(1, 1) if case == "periodic" else (0, 0),
+                   boundary_lo=("reflecting", "reflecting"), boundary_hi=("reflecting", "reflecting"))
+    dom = dict(lvd)
+    U1, U0 = _coarsen(U2, 1), _coarsen(U2, 2)
+    acts = [None, np.ones((2 * ny // B, 2 * nx // B), np.uint8), np.ones((4 * ny // B, 4 * nx // B), np.uint8)]
+    h = amr_oracle.Hierarchy([U0, U1, U2], acts, dom, B, chemistry=(case != "wedge"))
+    g2 = h.g[2]
+    dt = 0.3 * oracle.cfl_dt(g2, oracle.fill_ghosts(g2, oracle.ghosted(U2)), 1.0)
+    for _ in range(2):
+        h.step(dt)
+    ref = U2
+    Ug = oracle.fill_ghosts(g2, oracle.ghosted(U2))
+    for _ in range(2):
+        Ug, dta, st, _ = oracle.strang_step(g2, Ug, dt, chemistry=(case != "wedge"))
+        assert st == 0 and dta == dt
+    ref = Ug[2:-2, 2:-2]
+    assert np.array_equal(h.level(2), ref)
+    assert np.array_equal(h.level(1), _coarsen(ref, 1))
+    assert np.array_equal(h.level(0), _coarsen(h.level(1), 1))
+
+
+def test_three_levels_partial_refinement_conserves(oracle, amr_oracle):
+    nx, ny, B, dx = 32, 16, 8, 1e-4
+    U0 = H.smooth_field(nx, ny, seed=12)
+    crit = amr_oracle.criteria(box=(0.0008, 0.0016, 0.0004, 0.0012), box_only=True, chemistry=False)
+    dom = dict(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(1, 1))
+    h = amr_oracle.Hierarchy.from_base(U0, dom, B, crit, max_level=2, tag_buffer=1, chemistry=True)
+    assert h.finest == 2 and 0 < h.acts[2].sum() < h.acts[2].size
+    # proper nesting: every level-2 block's footprint grown by 2 lies in active level-1 cells
+    a1 = np.kron(h.acts[1], np.ones((B, B), np.uint8)).astype(bool)
+    for bj, bi in zip(*np.nonzero(h.acts[2])):
+        rows = np.arange(bj * B // 2 - 2, (bj + 1) * B // 2 + 2) % a1.shape[0]
+        cols = np.arange(bi * B // 2 - 2, (bi + 1) * B // 2 + 2) % a1.shape[1]
+        assert a1[np.ix_(rows, cols)].all()
+    g = oracle.make_grid(4 * nx, 4 * ny, dx / 4, dx / 4, periodic=(1, 1))
+    dt = 0.3 * oracle.cfl_dt(g, oracle.fill_ghosts(g, oracle.ghosted(np.kron(U0, np.ones((4, 4, 1))))), 1.0)
+    t0 = h.totals()
+    for _ in range(2):
+        h.step(dt)
+    t1 = h.totals()
+    ns = U0.shape[2] - 3
+    mass = t0[:ns].sum()
+    assert abs(t1[:ns].sum() - mass) <= 1e-13 * mass
+    assert abs(t1[ns + 2] - t0[ns + 2]) <= 1e-12 * abs(t0[ns + 2])
+
+
+def test_walled_partial_refinement_conserves(oracle, amr_oracle):
+    """Reflecting walls on all sides and level-1 blocks on two of them: mass and energy
+    stay, the wall faces of the blocks carry no mass flux."""
+    nx, ny, B, dx = 32, 16, 8, 1e-4
+    U0 = H.smooth_field(nx, ny, seed=13)
+    U1 = H.smooth_field(2 * nx, 2 * ny, seed=14)
+    act = np.zeros((2 * ny // B, 2 * nx // B), np.uint8)
+    act[0, :3] = 1      # along the bottom wall from the left wall
+    act[3, 5:] = 1      # along the top wall to the right wall
+    dom = dict(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+               boundary_hi=("reflecting", "reflecting"))
+    h = amr_oracle.Hierarchy([U0, U1], [None, act], dom, B, chemistry=True)
+    g = oracle.make_grid(2 * nx, 2 * ny, dx / 2, dx / 2)
+    dt = 0.3 * oracle.cfl_dt(g, oracle.fill_ghosts(g, oracle.ghosted(U1)), 1.0)
+    t0 = h.totals()
+    for _ in range(2):
+        h.step(dt)
+    t1 = h.totals()
+    ns = U0.shape[2] - 3
+    mass = t0[:ns].sum()
+    assert abs(t1[:ns].sum() - mass) <= 1e-13 * mass
+    assert abs(t1[ns + 2] - t0[ns + 2]) <= 1e-12 * abs(t0[ns + 2])
