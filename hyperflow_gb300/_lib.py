@@ -86,6 +86,7 @@ SIGNATURES = [
     ("hf_amr_create", _i32, [_vp, ctypes.POINTER(Level), _vp, ctypes.POINTER(AmrOpts), ctypes.POINTER(_vp), _vp]),
     ("hf_amr_destroy", None, [_vp]),
     ("hf_amr_step", _i32, [_vp, _d, _dp, _vp]),
+    ("hf_amr_cfl_dt", _i32, [_vp, _d, _dp, _vp]),
     ("hf_amr_regrid", _i32, [_vp, _vp]),
     ("hf_amr_info", _i32, [_vp, ctypes.c_int, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                            ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i64)]),

@@ -778,6 +778,21 @@ void hf_amr_destroy(hf_amr* m) {
     delete m;
 }
 
+hf_status hf_amr_cfl_dt(hf_amr* m, double cfl, double* dt, void* stream) {
+    if (!m || !dt || !(cfl > 0)) return HF_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    double h = INFINITY;
+    for (int l = 0; l <= m->finest; ++l) {
+        AmrLevel& a = m->lev[l];
+        double d = 0.0;
+        const hf_status r = hf_cfl_dt(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), a.U, cfl, &d, s);
+        if (r != HF_OK) return r;
+        h = std::min(h, d);
+    }
+    *dt = h;
+    return HF_OK;
+}
+
 hf_status hf_amr_step(hf_amr* m, double cfl, double* dt, void* stream) {
     if (!m || !dt) return HF_ERR_ARG;
     const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

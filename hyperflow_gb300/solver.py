@@ -660,7 +660,6 @@ class AmrStepper:
         o.rtol, o.atol = float(rtol), float(atol)
         o.tags = tag_criteria(chemistry=chemistry, **(tags or {}))
         self.opts = o
-        self.base = level
         self.nv = U0.shape[0]
         h = ctypes.c_void_p()
         torch.cuda.synchronize()
@@ -712,30 +711,10 @@ class AmrStepper:
 
     def cfl_dt(self, cfl=0.5):
         """stableDt over the active cells of every level (BlockAMR.cpp:335-346), the step
-        hf_amr_step takes when given dt <= 0: hf_cfl_dt over each level's active blocks
-        (a maximum of cell rates, so the patch split does not change it)."""
-        finest = self.info(0)["finest"]
-        rate_dt = float("inf")
-        for lev in range(finest + 1):
-            i = self.info(lev)
-            U, act = self.level(lev)
-            block = self.opts.block
-            boxes = [(bi * block, bj * block, min((bi + 1) * block, i["nx"]) - 1, min((bj + 1) * block, i["ny"]) - 1)
-                     for bj, bi in zip(*np.nonzero(act))]
-            if not boxes:
-                continue
-            ps = PatchSet(self.nv, boxes, device=U.device)
-            for k, (i0, j0, i1, j1) in enumerate(boxes):
-                ps.interior(k).copy_(U[:, j0:j1 + 1, i0:i1 + 1])
-            lv = L.Level()
-            ctypes.memmove(ctypes.byref(lv), ctypes.byref(self.base), ctypes.sizeof(L.Level))
-            lv.nx, lv.ny = i["nx"], i["ny"]
-            lv.dx, lv.dy = self.base.dx / (1 << lev), self.base.dy / (1 << lev)
-            d = ctypes.c_double(0.0)
-            self.ctx.check(self.ctx.lib.hf_cfl_dt(self.ctx.h, ctypes.byref(lv), ps.patches, len(ps), _ptr(ps.data),
-                                                  float(cfl), ctypes.byref(d), _stream()), "cfl_dt")
-            rate_dt = min(rate_dt, d.value)
-        return rate_dt
+        hf_amr_step takes when given dt <= 0 on its host-driven path."""
+        d = ctypes.c_double(0.0)
+        self.ctx.check(self.ctx.lib.hf_amr_cfl_dt(self.h, float(cfl), ctypes.byref(d), _stream()), "amr_cfl_dt")
+        return d.value
 
     @property
     def time(self):

@@ -355,6 +355,9 @@ HF_EXPORT hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const doubl
 HF_EXPORT void hf_amr_destroy(hf_amr* amr);
 /* One Strang step of every level; *dt as hf_stepper_step (<= 0: stableDt over all levels). */
 HF_EXPORT hf_status hf_amr_step(hf_amr* amr, double cfl, double* dt, void* stream);
+/* BlockAMR::stableDt (BlockAMR.cpp:335-346) over the active cells of every level: the
+ * step hf_amr_step takes when given *dt <= 0 on its host-driven path. */
+HF_EXPORT hf_status hf_amr_cfl_dt(hf_amr* amr, double cfl, double* dt, void* stream);
 HF_EXPORT hf_status hf_amr_regrid(hf_amr* amr, void* stream);
 /* Level sizes, block grid, finest level and the level's leaf cells. */
 HF_EXPORT hf_status hf_amr_info(const hf_amr* amr, int lev, int32_t* nx, int32_t* ny, int32_t* nbx, int32_t* nby,
