@@ -2,7 +2,9 @@
 a block hierarchy tile the domain once (the geometry check of
 HyperFlow_V3/tests/validate.py:64-78), their conserved sums are the hierarchy's leaf
 totals, and state_N.csv / boxes_N.csv read back the way the reference's scripts read
-them.  The hierarchy comes from the composite AMR oracle."""
+them.  The hierarchy comes from the composite AMR oracle, which also stands in for the
+GPU stepper to check run_amr_case's host logic (output times, regrid cadence, history,
+summary)."""
 import numpy as np
 import pytest
 
@@ -91,3 +93,94 @@ def test_state_rows_of_the_oracle_hierarchy(oracle, out, tmp_path):
     assert len(boxes) == 1 + int(active.sum())
     assert abs(np.sum((boxes["x_right"] - boxes["x_left"]) * (boxes["y_top"] - boxes["y_bottom"])
                       * (boxes["level"] == 1)) - active.sum() * (B * dx / 2) ** 2) < 1e-18
+
+
+class OracleAmr:
+    """AmrStepper's interface over the composite oracle (regrids driven by the caller)."""
+
+    def __init__(self, oracle, amr, U0, lvd, block, crit, max_level, tag_buffer):
+        self.o, self.B = oracle, block
+        self.h = amr.Hierarchy.from_base(U0, lvd, block, crit, max_level=max_level, tag_buffer=tag_buffer,
+                                         regrid_interval=0, chemistry=False)
+
+    def info(self, lev):
+        h = self.h
+        (ny, nx), (nby, nbx) = h.shape[lev], h.nb[lev]
+        leaf = int(h.leaf_mask(lev).sum()) if lev <= h.finest else 0
+        return dict(nx=nx, ny=ny, nbx=nbx, nby=nby, finest=h.finest, leaf_cells=leaf)
+
+    def level(self, lev):
+        import torch
+        h = self.h
+        act = h.acts[lev] if lev <= h.finest else np.zeros_like(h.acts[lev])
+        return torch.from_numpy(np.ascontiguousarray(h.level(lev).transpose(2, 0, 1))), act.copy()
+
+    def cfl_dt(self, cfl):
+        h, o, B = self.h, self.o, self.B
+        dts = [o.cfl_dt(h.g[0], o.fill_ghosts(h.g[0], h.X[0].copy()), cfl)]
+        for lev in range(1, h.finest + 1):
+            for bi, bj in h.blocks(lev):
+                win = h.X[lev][bj * B:bj * B + B + 4, bi * B:bi * B + B + 4]
+                dts.append(o.cfl_dt(h._grid(lev, bi * B, bj * B, B, B), win, cfl))
+        return min(dts)
+
+    def step(self, dt=0.0, cfl=0.5):
+        self.h.step(dt)
+        return dt
+
+    def regrid(self):
+        self.h.regrid()
+
+    def totals(self):
+        return self.h.totals()
+
+    def close(self):
+        pass
+
+
+class CountingCtx:
+    def counters(self):
+        return {"retries": 0, "first_order_stages": 0, "roundoff_repairs": 0, "chem_cell_calls": 0}
+
+
+def test_run_amr_case_host_logic(oracle, out, tmp_path):
+    """run_amr_case over the composite oracle: the reference's files at t = 0 and at two
+    output times, leaf cells tiling the domain on three levels, one history row per
+    step, a regrid after every second step except one that reached the end time
+    (BlockAMR.cpp:420), and conserved totals on the periodic box."""
+    import json
+    import amr
+    import torch
+    from hyperflow_gb300 import solver as S
+    nx, ny, B, dx = 32, 16, 8, 1e-4
+    U0 = H.smooth_field(nx, ny, seed=15)
+    lvd = dict(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(1, 1))
+    g = oracle.make_grid(4 * nx, 4 * ny, dx / 4, dx / 4, periodic=(1, 1))
+    dt = 0.5 * oracle.cfl_dt(g, oracle.fill_ghosts(g, oracle.ghosted(np.kron(U0, np.ones((4, 4, 1))))), 1.0)
+    kw = dict(box=(0.0008, 0.0016, 0.0004, 0.0012), box_only=True, velocity=(2 * dx / (2 * dt), 0.0))
+    stepper = OracleAmr(oracle, amr, U0, lvd, B, amr.criteria(chemistry=False, **kw), 2, 1)
+
+    def props(q):
+        p, _, T, st = oracle.properties(np.ascontiguousarray(q.T))
+        assert not np.any(st)
+        return p, T
+
+    end = 5.5 * dt
+    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0.transpose(2, 0, 1).copy()), end,
+                         str(tmp_path), cfl=0.5, output_times=[2.5 * dt, end], max_level=2, block=B, tag_buffer=1,
+                         regrid_interval=2, chemistry=False, stepper=stepper, props=props)
+    import os
+    assert sorted(os.listdir(tmp_path)) == ["boxes_0.csv", "boxes_1.csv", "boxes_2.csv", "history.csv",
+                                            "state_0.csv", "state_1.csv", "state_2.csv", "summary.json"]
+    assert s["final_time"] == end and s["finest_level"] == 2
+    steps = s["steps"]
+    assert s["regrids"] == sum(1 for k in range(1, steps) if k % 2 == 0)
+    for k in range(3):
+        data = np.genfromtxt(tmp_path / ("state_%d.csv" % k), names=True, delimiter=",")
+        check_geometry(data, (nx, ny), (nx * dx, ny * dx), 2)
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+    hist = np.genfromtxt(tmp_path / "history.csv", names=True, delimiter=",")
+    assert len(hist) == steps + 1 and hist["regrids"][-1] == s["regrids"] and hist["finest_level"][-1] == 2
+    assert abs(hist["t"][-1] - end) == 0 and np.all(np.diff(hist["t"]) > 0)
