@@ -15,9 +15,10 @@ on levels 0..max_level of a domain with the reference's boundary conditions.
 - Euler stage: level 0 as one box, level l >= 1 block by block (a block face is a wall
   face only where it lies on a reflecting or wedge domain edge), then from the finest
   level down: reflux of level l-1 from level l's face fluxes (FluxRegister, :245-256)
-  and average_down (:256).  Not restated: the first-order redo and the roundoff repair
-  (an inadmissible stage or a negative species raises; the cases compared never need
-  them).
+  and average_down (:256).  A stage whose updated cells are inadmissible on any level
+  is redone first order on every level (:258-263).  Not restated: the roundoff repair
+  of species slightly below zero (within 64 ulp of their peak; they raise, and the cases
+  compared never produce them).
 - flow(h): two stages, Heun combination, average_down, validation.
 - react(dt): the leaf cells of every level through the oracle's ChemistryBatch, then
   average_down.
@@ -100,7 +101,7 @@ class Hierarchy:
                 self.finest = l
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
         self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
-        self.time, self.steps, self.regrids = 0.0, 0, 0
+        self.time, self.steps, self.regrids, self.first_order_stages = 0.0, 0, 0, 0
         self._rebuild()
         self.X = self.average_all(self.X)
 
@@ -216,15 +217,16 @@ class Hierarchy:
             if np.any(oracle.properties(self._active_cells(X, l))[3]):
                 raise RuntimeError("inadmissible level-%d cell after %s" % (l, what))
 
-    def euler(self, Xin, h):
-        Xin = self.fill([x.copy() for x in Xin])
+    def _stages(self, Xin, h, first_order):
+        """Every level's Euler update from the filled Xin: (out, whole-level face fluxes,
+        per-block fine fluxes, admissible)."""
         out = [x.copy() for x in Xin]
         B = self.B
         FX, FY, fine = [], [], []
         for l in range(self.finest + 1):
             ny, nx = self.shape[l]
             if l == 0:
-                o, fx, fy, st = oracle.euler_stage(self.g[0], Xin[0], h)
+                o, fx, fy, st = oracle.euler_stage(self.g[0], Xin[0], h, first_order)
                 if st:
                     raise RuntimeError("level-0 face inadmissible")
                 out[0][2:-2, 2:-2] = o[2:-2, 2:-2]
@@ -236,7 +238,8 @@ class Hierarchy:
             boxes, fxl, fyl = [], [], []
             for bi, bj in self.blocks(l):
                 i0, j0 = bi * B, bj * B
-                o, fx, fy, st = oracle.euler_stage(self._grid(l, i0, j0, B, B), Xin[l][j0:j0 + B + 4, i0:i0 + B + 4], h)
+                o, fx, fy, st = oracle.euler_stage(self._grid(l, i0, j0, B, B), Xin[l][j0:j0 + B + 4, i0:i0 + B + 4], h,
+                                                   first_order)
                 if st:
                     raise RuntimeError("level-%d face inadmissible" % l)
                 out[l][j0 + 2:j0 + 2 + B, i0 + 2:i0 + 2 + B] = o[2:-2, 2:-2]
@@ -248,7 +251,35 @@ class Hierarchy:
             FX.append(fxa)
             FY.append(fya)
             fine.append((boxes, fxl, fyl))
-        self._check(out, "a stage")
+        ok = all(self._stage_ok(out, l) for l in range(self.finest + 1))
+        return out, FX, FY, fine, ok
+
+    def _stage_ok(self, X, l):
+        """The per-level check after an update (BlockAMR.cpp:286-334): a species below
+        -64 eps x its peak (or not finite) fails the stage, a smaller negative one would be
+        repaired (not restated here: raises), an inadmissible cell fails the stage."""
+        cells = self._active_cells(X, l)
+        ns = self.nv - 3
+        sp = cells[:, :ns]
+        if np.any(~np.isfinite(sp)):
+            return False
+        neg = sp < 0
+        if neg.any():
+            if np.any(-sp > 64 * np.finfo(np.float64).eps * sp.max(0)):
+                return False
+            raise RuntimeError("level-%d roundoff repair needed (not restated)" % l)
+        return not np.any(oracle.properties(cells)[3])
+
+    def euler(self, Xin, h):
+        """One composite stage: second order, or first order on every level when a level's
+        updated cells are inadmissible (BlockAMR.cpp:258-263)."""
+        Xin = self.fill([x.copy() for x in Xin])
+        out, FX, FY, fine, ok = self._stages(Xin, h, False)
+        if not ok:
+            out, FX, FY, fine, ok = self._stages(Xin, h, True)
+            if not ok:
+                raise RuntimeError("inadmissible cell after a first-order stage")
+            self.first_order_stages += 1
         for l in range(self.finest, 0, -1):
             boxes, fxl, fyl = fine[l]
             dx, dy = self.dxs[l - 1]
