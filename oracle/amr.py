@@ -16,9 +16,8 @@ on levels 0..max_level of a domain with the reference's boundary conditions.
   face only where it lies on a reflecting or wedge domain edge), then from the finest
   level down: reflux of level l-1 from level l's face fluxes (FluxRegister, :245-256)
   and average_down (:256).  A stage whose updated cells are inadmissible on any level
-  is redone first order on every level (:258-263).  Not restated: the roundoff repair
-  of species slightly below zero (within 64 ulp of their peak; they raise, and the cases
-  compared never produce them).
+  is redone first order on every level (:258-263); species below zero by at most 64
+  ulp of their peak are repaired first, level by level (repairRoundoff, :299-334).
 - flow(h): two stages, Heun combination, average_down, validation.
 - react(dt): the leaf cells of every level through the oracle's ChemistryBatch, then
   average_down.
@@ -101,7 +100,7 @@ class Hierarchy:
                 self.finest = l
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
         self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
-        self.time, self.steps, self.regrids, self.first_order_stages = 0.0, 0, 0, 0
+        self.time, self.steps, self.regrids, self.first_order_stages, self.roundoff_repairs = 0.0, 0, 0, 0, 0
         self._rebuild()
         self.X = self.average_all(self.X)
 
@@ -255,19 +254,46 @@ class Hierarchy:
         return out, FX, FY, fine, ok
 
     def _stage_ok(self, X, l):
-        """The per-level check after an update (BlockAMR.cpp:286-334): a species below
-        -64 eps x its peak (or not finite) fails the stage, a smaller negative one would be
-        repaired (not restated here: raises), an inadmissible cell fails the stage."""
-        cells = self._active_cells(X, l)
-        ns = self.nv - 3
+        """The per-level check after an update (repairRoundoff and validate,
+        BlockAMR.cpp:286-334, over the level's active cells in block order): a species
+        below zero by at most 64 ulp of its peak is zeroed and its mass taken from the
+        first cell holding the peak; a larger or non-finite negative value, or a donor
+        too small, fails the stage, and so does an inadmissible cell.  X[l] is repaired
+        in place."""
+        B, ns = self.B, self.nv - 3
+        if l == 0:
+            views = [X[0][2:-2, 2:-2]]
+        else:
+            views = [X[l][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B] for bi, bj in self.blocks(l)]
+        cells = np.concatenate([v.reshape(-1, self.nv) for v in views])
         sp = cells[:, :ns]
-        if np.any(~np.isfinite(sp)):
-            return False
-        neg = sp < 0
-        if neg.any():
-            if np.any(-sp > 64 * np.finfo(np.float64).eps * sp.max(0)):
+        if np.any(sp < 0) or np.any(~np.isfinite(sp)):
+            dx, dy = self.dxs[l]
+            vol = dx * dy
+            peak = np.where(sp > 0, sp, 0.0).max(0)
+            bad = ~np.isfinite(sp) | ((sp < 0) & (-sp > 64 * np.finfo(np.float64).eps * peak))
+            if bad.any():
                 return False
-            raise RuntimeError("level-%d roundoff repair needed (not restated)" % l)
+            deficit, count = np.zeros(ns), 0
+            for n in range(ns):
+                neg = np.nonzero(sp[:, n] < 0)[0]
+                if not len(neg):
+                    continue
+                for k in neg:
+                    deficit[n] += -sp[k, n] * vol
+                    sp[k, n] = 0.0
+                count += len(neg)
+                if not peak[n] * vol > deficit[n]:
+                    return False
+                donor = int(np.nonzero(sp[:, n] == peak[n])[0][0])
+                sp[donor, n] -= deficit[n] / vol
+            cells[:, :ns] = sp
+            k = 0
+            for v in views:
+                n = v.shape[0] * v.shape[1]
+                v[:] = cells[k:k + n].reshape(v.shape)
+                k += n
+            self.roundoff_repairs += count
         return not np.any(oracle.properties(cells)[3])
 
     def euler(self, Xin, h):

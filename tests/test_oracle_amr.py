@@ -223,3 +223,28 @@ def test_walled_partial_refinement_conserves(oracle, amr_oracle):
     mass = t0[:ns].sum()
     assert abs(t1[:ns].sum() - mass) <= 1e-13 * mass
     assert abs(t1[ns + 2] - t0[ns + 2]) <= 1e-12 * abs(t0[ns + 2])
+
+
+def test_stage_check_repairs_roundoff_negatives(oracle, amr_oracle):
+    """repairRoundoff on a block level: a species a few ulp below zero is zeroed and its
+    mass taken from the first cell holding the level's peak; one far below zero fails
+    the stage (BlockAMR.cpp:299-334)."""
+    nx, ny, B, dx = 32, 16, 8, 1e-4
+    U0 = H.smooth_field(nx, ny, seed=5)
+    U1 = H.smooth_field(2 * nx, 2 * ny, seed=6)
+    active = np.zeros((2 * ny // B, 2 * nx // B), np.uint8)
+    active[:, 2:5] = 1
+    a = amr_oracle.AmrOracle(U0, U1, active, dx, dx, B)
+    X = [x.copy() for x in a.X]
+    lv = X[1][2:-2, 2:-2]
+    cells = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12) for bi, bj in a.blocks(1)])
+    peak = cells[:, 5].max()
+    lv[3, 20, 5] = -2e-16 * peak      # within 64 ulp: repaired
+    total = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12)
+                            for bi, bj in a.blocks(1)])[:, 5].sum()
+    assert a._stage_ok(X, 1)
+    assert lv[3, 20, 5] == 0.0 and a.roundoff_repairs == 1
+    cells = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12) for bi, bj in a.blocks(1)])
+    assert abs(cells[:, 5].sum() - total) <= 1e-14 * total
+    lv[5, 22, 5] = -1e-3 * peak       # materially negative: the stage fails
+    assert not a._stage_ok(X, 1)
