@@ -19,6 +19,8 @@ on levels 0..max_level of a domain with the reference's boundary conditions.
   is redone first order on every level (:258-263); species below zero by at most 64
   ulp of their peak are repaired first, level by level (repairRoundoff, :299-334).
 - flow(h): two stages, Heun combination, average_down, validation.
+- step(dt): flow(dt/2), react(dt), flow(dt/2); a failed attempt is rolled back and
+  retried with half the step (:411-419).
 - react(dt): the leaf cells of every level through the oracle's ChemistryBatch, then
   average_down.
 - regrid (every regrid_interval steps, and max_level times to build the initial
@@ -51,6 +53,11 @@ def criteria(pressure_tag=0.08, temperature_tag=0.08, fuel_rate_tag=50.0, densit
             c.box[k] = float(box[k])
     c.velocity[0], c.velocity[1] = float(velocity[0]), float(velocity[1])
     return c
+
+
+class StepFailure(RuntimeError):
+    """A failure that BlockAMR::run answers with a rollback and a halved dt
+    (BlockAMR.cpp:413-418): an inadmissible face or cell, a failed chemistry cell."""
 
 
 def _wrap(n, count, periodic):
@@ -100,7 +107,8 @@ class Hierarchy:
                 self.finest = l
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
         self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
-        self.time, self.steps, self.regrids, self.first_order_stages, self.roundoff_repairs = 0.0, 0, 0, 0, 0
+        self.time, self.steps, self.regrids, self.retries = 0.0, 0, 0, 0
+        self.first_order_stages, self.roundoff_repairs = 0, 0
         self._rebuild()
         self.X = self.average_all(self.X)
 
@@ -214,7 +222,7 @@ class Hierarchy:
     def _check(self, X, what):
         for l in range(self.finest + 1):
             if np.any(oracle.properties(self._active_cells(X, l))[3]):
-                raise RuntimeError("inadmissible level-%d cell after %s" % (l, what))
+                raise StepFailure("inadmissible level-%d cell after %s" % (l, what))
 
     def _stages(self, Xin, h, first_order):
         """Every level's Euler update from the filled Xin: (out, whole-level face fluxes,
@@ -227,7 +235,7 @@ class Hierarchy:
             if l == 0:
                 o, fx, fy, st = oracle.euler_stage(self.g[0], Xin[0], h, first_order)
                 if st:
-                    raise RuntimeError("level-0 face inadmissible")
+                    raise StepFailure("level-0 face inadmissible")
                 out[0][2:-2, 2:-2] = o[2:-2, 2:-2]
                 FX.append(fx)
                 FY.append(fy)
@@ -240,7 +248,7 @@ class Hierarchy:
                 o, fx, fy, st = oracle.euler_stage(self._grid(l, i0, j0, B, B), Xin[l][j0:j0 + B + 4, i0:i0 + B + 4], h,
                                                    first_order)
                 if st:
-                    raise RuntimeError("level-%d face inadmissible" % l)
+                    raise StepFailure("level-%d face inadmissible" % l)
                 out[l][j0 + 2:j0 + 2 + B, i0 + 2:i0 + 2 + B] = o[2:-2, 2:-2]
                 fxa[j0:j0 + B, i0:i0 + B + 1] = fx
                 fya[j0:j0 + B + 1, i0:i0 + B] = fy
@@ -304,7 +312,7 @@ class Hierarchy:
         if not ok:
             out, FX, FY, fine, ok = self._stages(Xin, h, True)
             if not ok:
-                raise RuntimeError("inadmissible cell after a first-order stage")
+                raise StepFailure("inadmissible cell after a first-order stage")
             self.first_order_stages += 1
         for l in range(self.finest, 0, -1):
             boxes, fxl, fyl = fine[l]
@@ -331,7 +339,7 @@ class Hierarchy:
         batch = np.concatenate([self.X[l][2:-2, 2:-2][masks[l]] for l in range(self.finest + 1)])
         out, bad, _ = oracle.chem_batch(batch, dt, rtol=self.rtol, atol=self.atol)
         if bad >= 0:
-            raise RuntimeError("chemistry cell %d failed" % bad)
+            raise StepFailure("chemistry cell %d failed" % bad)
         k = 0
         for l in range(self.finest + 1):
             n = int(masks[l].sum())
@@ -341,13 +349,27 @@ class Hierarchy:
         self._check(self.X, "react")
 
     def step(self, dt):
-        self.flow(0.5 * dt)
-        self.react(dt)
-        self.flow(0.5 * dt)
-        self.time += dt
+        """One Strang step of every level; a failed attempt is rolled back and retried with
+        half the step, at most 18 attempts (BlockAMR.cpp:411-419).  Returns the step taken."""
+        backup = [x.copy() for x in self.X]
+        h = dt
+        for _ in range(18):
+            try:
+                self.flow(0.5 * h)
+                self.react(h)
+                self.flow(0.5 * h)
+                break
+            except StepFailure:
+                self.X = [x.copy() for x in backup]
+                self.retries += 1
+                h *= 0.5
+        else:
+            raise RuntimeError("time advancement failed")
+        self.time += h
         self.steps += 1
         if self.interval > 0 and self.steps % self.interval == 0:
             self.regrid()
+        return h
 
     # ------------------------------------------------------------ regrid
     def _regrid_level(self, l):

@@ -248,3 +248,19 @@ def test_stage_check_repairs_roundoff_negatives(oracle, amr_oracle):
     assert abs(cells[:, 5].sum() - total) <= 1e-14 * total
     lv[5, 22, 5] = -1e-3 * peak       # materially negative: the stage fails
     assert not a._stage_ok(X, 1)
+
+
+def test_rollback_halves_like_the_one_level_run(oracle, amr_oracle):
+    """Fully refined, a step 8 times the CFL step fails and is retried with half the step
+    until it passes (BlockAMR.cpp:411-419): the step taken and the fine level equal the
+    one-level oracle's run of the fine grid bit for bit."""
+    nx, ny, B, dx = 16, 8, 8, 1e-4
+    U1 = H.smooth_field(2 * nx, 2 * ny, seed=3)
+    U0 = oracle.average_down(U1)
+    a = amr_oracle.AmrOracle(U0, U1, np.ones((2 * ny // B, 2 * nx // B), np.uint8), dx, dx, B, chemistry=False)
+    dt = 8.0 * fine_dt(oracle, U1, dx, dx, cfl=1.0)
+    h = a.step(dt)
+    g = oracle.make_grid(2 * nx, 2 * ny, dx / 2, dx / 2, periodic=(1, 1))
+    Ug, dta, st, _ = oracle.strang_step(g, oracle.fill_ghosts(g, oracle.ghosted(U1)), dt, chemistry=False)
+    assert st == 0 and h == dta < dt and a.retries >= 1
+    assert np.array_equal(a.level(1), Ug[2:-2, 2:-2])

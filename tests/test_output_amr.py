@@ -125,8 +125,7 @@ class OracleAmr:
         return min(dts)
 
     def step(self, dt=0.0, cfl=0.5):
-        self.h.step(dt)
-        return dt
+        return self.h.step(dt)
 
     def regrid(self):
         self.h.regrid()
