@@ -311,3 +311,33 @@ def test_amr_three_level_wedge_matches_composite_oracle(gpu, oracle):
     for got, ref in pairs:
         assert np.max(np.abs(got - ref) / scale) < 1e-9
     m.close()
+
+
+def test_amr_rollback_matches_composite_oracle(gpu, oracle):
+    """Two periodic levels with part of level 1 active, one step of 8 times the CFL step
+    on the host-driven path: the GPU stepper and the composite oracle roll back and
+    halve to the same step, and their levels agree to 1e-10 of each component's physical
+    scale (flux path only)."""
+    import amr
+    import hyperflow_gb300 as hf
+    nx, ny, B, dx = 32, 16, 8, 1e-4
+    U0 = H.smooth_field(nx, ny, seed=7)
+    crit = dict(box=(0.0008, 0.0016, -1.0, 1.0), box_only=True)
+    m = hf.AmrStepper(gpu, hf.make_level(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(1, 1)), cuda(U0.transpose(2, 0, 1)),
+                      max_level=1, block=B, tag_buffer=1, regrid_interval=0, chemistry=False, tags=crit)
+    o = amr.AmrOracle.from_base(U0, dx, dx, B, amr.criteria(chemistry=False, **crit), tag_buffer=1, chemistry=False)
+    assert np.array_equal(m.level(1)[1], o.active) and 0 < o.active.sum() < o.active.size
+    dt = 8.0 * m.cfl_dt(1.0)
+    h = m.step(dt=dt)
+    assert h < dt and o.step(dt) == h
+    pairs = [(m.level(0)[0].cpu().numpy().transpose(1, 2, 0).reshape(-1, 12), o.level(0).reshape(-1, 12))]
+    G1, R1 = m.level(1)[0].cpu().numpy().transpose(1, 2, 0), o.level(1)
+    for bj, bi in zip(*np.nonzero(o.active)):
+        sl = (slice(bj * B, (bj + 1) * B), slice(bi * B, (bi + 1) * B))
+        pairs.append((G1[sl].reshape(-1, 12), R1[sl].reshape(-1, 12)))
+    ref_all = np.concatenate([r for _, r in pairs])
+    rho = ref_all[:, :9].sum(1).max()
+    scale = np.array([rho] * 9 + [rho * 1000.0] * 2 + [np.abs(ref_all[:, 11]).max()])
+    for got, ref in pairs:
+        assert np.max(np.abs(got - ref) / scale) < 1e-10
+    m.close()
