@@ -13,8 +13,6 @@ import numpy as np
 import pytest
 import torch
 
-import helpers as H
-
 pytestmark = pytest.mark.gpu
 
 

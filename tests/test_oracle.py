@@ -7,7 +7,6 @@ is checked by identities and by the tolerances of the reference's own tests
 (validate.py:140-159, docs/amr_checks.json).
 """
 import numpy as np
-import pytest
 
 import helpers as H
 
