@@ -1,10 +1,10 @@
 """The CPU oracle against the reference's known answers and against identities.
 
 The only exact known-answer vectors the reference holds for this path are the
-ghost values of HyperFlow_V3/tests/boundary_check.cpp; the thermo/kinetics
-restatement of Cantera cannot be pinned numerically here (Cantera absent), so it
-is checked by identities and by the tolerances of the reference's own tests
-(validate.py:140-159, docs/amr_checks.json).
+ghost values of HyperFlow_V3/tests/boundary_check.cpp.  The thermo/kinetics
+restatement of Cantera (absent here) is checked by identities and by the tolerances
+of the reference's own tests (validate.py:140-159, docs/amr_checks.json) in this
+file, and against the reference's recorded run outcomes in test_oracle_cases.py.
 """
 import numpy as np
 
