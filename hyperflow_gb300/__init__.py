@@ -6,9 +6,9 @@ reference's per-block names (see solver.py).  There is no CPU fallback.
 """
 from .solver import (AmrStepper, ChemistryBatch, ChemObjective, ChemSensitivity, ConservativeInterp, Context,  # noqa
                      DomainError, FlowAdjoint, HyperFlowError, PatchArray, PatchSet, Stepper, admissible,
-                     average_down, cfl_dt, euler_stage, fill, hllc, induction_length, make_level, properties, reflux,
-                     tag_cells, totals, validate)
+                     average_down, cfl_dt, euler_stage, fill, flux_adjoint, hllc, induction_length, make_level,
+                     properties, reflux, tag_cells, totals, validate)
 
 __all__ = ["AmrStepper", "ChemistryBatch", "ChemObjective", "ChemSensitivity", "ConservativeInterp", "Context", "DomainError",
            "FlowAdjoint", "HyperFlowError", "induction_length", "PatchArray", "PatchSet", "Stepper", "admissible", "average_down", "cfl_dt", "euler_stage",
-           "fill", "hllc", "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]
+           "fill", "flux_adjoint", "hllc", "make_level", "properties", "reflux", "tag_cells", "totals", "validate"]

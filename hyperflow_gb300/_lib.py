@@ -99,6 +99,8 @@ SIGNATURES = [
                               ctypes.POINTER(_vp), _vp]),
     ("hf_flow_adjoint", _i32, [_vp, _vp, _vp, _vp, _vp]),
     ("hf_flow_tape_destroy", None, [_vp]),
+    ("hf_flux_adjoint", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), _vp, _vp, _d, ctypes.c_int, _vp,
+                               _vp]),
     ("hf_chem_objective", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp,
                                  ctypes.POINTER(_i64), _vp]),
     ("hf_chem_adjoint", _i32, [_vp, _vp, _i64, _i64, _d, _i32, ctypes.POINTER(AdjointOpts), _vp, _vp, _vp,

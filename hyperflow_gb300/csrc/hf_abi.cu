@@ -431,6 +431,30 @@ hf_status hf_flux_update(hf_ctx* ctx, const hf_level* level, const hf_patch* pat
     return HF_OK;
 }
 
+hf_status hf_flux_adjoint(hf_ctx* ctx, const hf_level* level, const hf_patch* patch, const double* U,
+                          const double* Ubar_out, double h, int first_order, double* Ubar_in, void* stream) {
+    if (!ctx || !level || !patch || !U || !Ubar_out || !Ubar_in || !level_ok(*level) || !patch_ok(*patch) || !(h > 0))
+        return fail(ctx, HF_ERR_ARG, "flux_adjoint: bad arguments");
+    const hf_patch& P = *patch;
+    if (P.ilo != 0 || P.jlo != 0 || P.nx != level->nx || P.ny != level->ny || P.ng != 2)
+        return fail(ctx, HF_ERR_ARG, "flux_adjoint: one domain-covering patch with 2 ghost layers");
+    for (int d = 0; d < 2; ++d)
+        if (level->bc_lo[d] == HF_BC_WEDGE || level->bc_hi[d] == HF_BC_WEDGE)
+            return fail(ctx, HF_ERR_ARG, "flux_adjoint: no wedge boundary");
+    const int nv = ctx->ns + 3;
+    const size_t nfa = 4 * (size_t)nv * (P.nx + 1) * P.ny, nfb = 4 * (size_t)nv * P.nx * (P.ny + 1);
+    const size_t nug = (size_t)P.offset + (size_t)nv * P.comp_stride;
+    double* w = static_cast<double*>(scratch(ctx, sizeof(double) * (nfa + nfb + nug)));
+    if (!w) return fail(ctx, HF_ERR_CUDA, "flux_adjoint: scratch allocation failed");
+    const cudaStream_t s = S(stream);
+    HF_CUDA(reset_status(ctx, s));
+    HF_CUDA(launch_stage_adjoint(ctx->ns, make_level(*level), P, U, Ubar_out, 1.0, h, first_order ? 1 : 0, w, w + nfa,
+                                 w + nfa + nfb, Ubar_in, ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(read_status(ctx, s));
+    if (ctx->st_host->flags & ST_FACE_BAD) return fail(ctx, HF_ERR_FACE, "flux_adjoint: inadmissible face state");
+    return HF_OK;
+}
+
 static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const int64_t* cell_index, int64_t count,
                              double dt, const double* dt_cell, double rtol, double atol, int form,
                              const hf_chem_history* hist, int64_t* first_failed, void* stream) {

@@ -220,6 +220,17 @@ def euler_stage(ctx, level, u_in, u_out, h, first_order=False, u_old=None, form=
     return fx, fy
 
 
+def flux_adjoint(ctx, level, u_in, ubar_out, h, first_order=False):
+    """Adjoint of one Euler stage (hf_flux_adjoint): u_in holds the forward stage's input
+    with its ghosts filled, ubar_out the cotangent of the stage output (same layout);
+    returns a PatchArray holding J^T ubar_out on the interior cells."""
+    out = u_in.like()
+    ctx.check(ctx.lib.hf_flux_adjoint(ctx.h, ctypes.byref(level), ctypes.byref(u_in.patch), _ptr(u_in.data),
+                                      _ptr(ubar_out.data), float(h), int(first_order), _ptr(out.data), _stream()),
+              "flux_adjoint")
+    return out
+
+
 def cfl_dt(ctx, level, patch_array, cfl):
     """stableDt (BlockAMR.cpp:335-346)."""
     dt = ctypes.c_double(0.0)

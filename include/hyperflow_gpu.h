@@ -258,6 +258,16 @@ HF_EXPORT hf_status hf_flow_record(hf_ctx* ctx, const hf_level* level, const dou
 HF_EXPORT hf_status hf_flow_adjoint(hf_flow_tape* tape, const double* seed, double* U0_bar, double* dJ_dlnA,
                                     void* stream);
 HF_EXPORT void hf_flow_tape_destroy(hf_flow_tape* tape);
+/* Adjoint of one Euler stage (the discrete transpose used by hf_flow_adjoint): for the map
+ * from a one-patch level's interior state U (ghosts filled from it by the boundary
+ * conditions) to the stage output U - h div F of hf_flux_update (no Heun combination;
+ * first_order as the forward stage took it), Ubar_in = J^T Ubar_out on the interior cells.
+ * U must hold the filled ghosts of the forward stage; U, Ubar_out and Ubar_in share the
+ * patch layout (one domain-covering patch, ng = 2).  No wedge boundary.  HF_ERR_FACE if a
+ * face state is inadmissible. */
+HF_EXPORT hf_status hf_flux_adjoint(hf_ctx* ctx, const hf_level* level, const hf_patch* patch, const double* U,
+                                    const double* Ubar_out, double h, int first_order, double* Ubar_in,
+                                    void* stream);
 
 /* Chemistry without any device allocation.  No counterpart in the reference.
  *

@@ -341,3 +341,48 @@ def test_amr_rollback_matches_composite_oracle(gpu, oracle):
     for got, ref in pairs:
         assert np.max(np.abs(got - ref) / scale) < 1e-10
     m.close()
+
+
+def test_flux_adjoint_matches_oracle_fd(gpu, oracle):
+    """hf_flux_adjoint (one Euler stage, walls left and at the top and bottom, periodic
+    nowhere, transmissive right): J^T w against kink-free central differences of
+    <w, stage(U)> from the oracle's stage at 24 sampled entries, the entries weighted by
+    the component's physical scale: 1e-5 relative (2-norm) and 1e-4 for each entry."""
+    import hyperflow_gb300 as hf
+    from test_gpu_flow_adjoint import clean_difference, scales
+    nx, ny, dx = 24, 12, 1e-4
+    A = H.smooth_field(nx, ny, seed=21)                  # (ny, nx, NV)
+    U = np.ascontiguousarray(A.transpose(2, 0, 1))       # (NV, ny, nx)
+    lvd = dict(nx=nx, ny=ny, dx=dx, dy=dx, periodic=(0, 0), boundary_lo=("reflecting", "reflecting"),
+               boundary_hi=("transmissive", "reflecting"))
+    level = hf.make_level(**lvd)
+    g = oracle.make_grid(nx, ny, dx, dx, periodic=(0, 0), bc_lo=(0, 0), bc_hi=(1, 0))
+    h = 0.3 * oracle.cfl_dt(g, oracle.fill_ghosts(g, oracle.ghosted(A)), 1.0)
+    sc = scales(U)
+    w = np.random.default_rng(5).uniform(-1.0, 1.0, U.shape) / sc[:, None, None]
+    pa = hf.PatchArray(12, nx, ny)
+    pa.interior().copy_(cuda(U))
+    hf.fill(gpu, level, pa)
+    wb = pa.like()
+    wb.interior().copy_(cuda(w))
+    G = hf.flux_adjoint(gpu, level, pa, wb, h).interior().cpu().numpy()
+
+    def J(V):
+        o, _, _, st = oracle.euler_stage(g, oracle.fill_ghosts(g, oracle.ghosted(V.transpose(1, 2, 0))), h)
+        assert st == 0
+        return float(np.sum(w * o[2:-2, 2:-2].transpose(2, 0, 1)))
+
+    J0 = J(U)
+    rng = np.random.default_rng(9)
+    got, want = [], []
+    while len(got) < 24:
+        n, j, i = int(rng.integers(0, 12)), int(rng.integers(0, ny)), int(rng.integers(0, nx))
+        i = [0, 1, nx - 2, nx - 1, i][int(rng.integers(0, 5))]  # boundary cells too
+        if n < 9 and U[n, j, i] <= 1e-5 * sc[n]:
+            continue  # a step of 1e-6 of the scale would make the partial density negative
+        fd = clean_difference(J, U, n, j, i, sc[n], J0, floor=1.0 / sc[n])
+        got.append(G[n, j, i] * sc[n])
+        want.append(fd * sc[n])
+    got, want = np.array(got), np.array(want)
+    assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
+    assert np.all(np.abs(got - want) <= 1e-4 * np.maximum(np.abs(want), 1.0))
