@@ -93,3 +93,20 @@ def test_every_struct_mirror_matches_header(tmp_path):
     subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == want
+
+
+def test_every_entry_point_rejects_null_arguments(lib):
+    """With null handles and pointers and zero sizes every status-returning entry point
+    returns HF_ERR_ARG before touching a device, and the others do nothing (no GPU is
+    needed for this)."""
+    from hyperflow_gb300 import _lib
+    for name, res, args in _lib.SIGNATURES:
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+        vals = [0.0 if a is ctypes.c_double else 0 if a in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64) else None
+                for a in args]
+        r = f(*vals)
+        if name == "hf_nspecies":
+            assert r == 0
+        elif res is _lib.SIGNATURES[0][1]:
+            assert r == _lib.HF_ERR_ARG, name
