@@ -85,6 +85,8 @@ SIGNATURES = [
     ("hf_fp64_peak", _i32, [_vp, _dp, _vp]),
     ("hf_amr_create", _i32, [_vp, ctypes.POINTER(Level), _vp, ctypes.POINTER(AmrOpts), ctypes.POINTER(_vp), _vp]),
     ("hf_amr_destroy", None, [_vp]),
+    ("hf_amr_create_levels", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(_vp), ctypes.c_int,
+                                    ctypes.POINTER(AmrOpts), ctypes.POINTER(_vp), _vp]),
     ("hf_amr_step", _i32, [_vp, _d, _dp, _vp]),
     ("hf_amr_cfl_dt", _i32, [_vp, _d, _dp, _vp]),
     ("hf_amr_regrid", _i32, [_vp, _vp]),

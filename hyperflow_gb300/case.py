@@ -134,3 +134,11 @@ def block_size(base_cells, max_grid_size=32):
         if base_cells[0] % (b // 2) == 0 and base_cells[1] % (b // 2) == 0:
             return b
     return None
+
+
+def levels(c, max_level=None):
+    """The initial state of levels 0..max_level (default: the case's max_level), each the
+    initial condition evaluated at that level's resolution (MakeNewLevelFromScratch,
+    BlockAMR.cpp:124-131): the U_levels of the block-AMR stepper."""
+    top = c.get("max_level", 2) if max_level is None else max_level
+    return [load(c, refine=lev)[0] for lev in range(top + 1)]

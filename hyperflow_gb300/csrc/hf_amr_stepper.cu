@@ -96,6 +96,7 @@ struct hf_amr {
     double graph_cfl = -1.0;
     int use_graph = 1, sm_count = 1;
     int64_t graph_steps = 0, host_steps = 0;
+    std::vector<const double*> init;  // per-level initial states while the hierarchy is built
 };
 
 namespace {
@@ -627,7 +628,10 @@ hf_status regrid_level(hf_amr* m, int l, cudaStream_t s) {
                 }
             next[(size_t)bj * f.nbx + bi] = nested ? 1 : 0;
         }
-    // blocks that become active: ConservativeInterp from level l
+    // blocks that become active: ConservativeInterp from level l, or, while the
+    // hierarchy is built, the caller's initial state of level l+1 when it gave one
+    // (MakeNewLevelFromScratch evaluates the initial condition on every level)
+    const double* init = l + 1 < (int)m->init.size() ? m->init[l + 1] : nullptr;
     std::vector<uint8_t> prev = f.active;
     const bool had = m->finest >= l + 1;
     f.active = next;
@@ -639,6 +643,17 @@ hf_status regrid_level(hf_amr* m, int l, cudaStream_t s) {
             const size_t b = (size_t)bj * f.nbx + bi;
             if (!next[b] || (had && prev[b])) continue;
             const hf_patch p = block_patch(f, bi, bj, B);
+            if (init) {
+                const int64_t nc = (int64_t)f.L.nx * f.L.ny;
+                for (int n = 0; n < m->nv; ++n)
+                    if (cudaMemcpy2DAsync(f.U + n * f.dom.comp_stride + (int64_t)(p.jlo + f.dom.ng) * f.dom.pitch +
+                                              (p.ilo + f.dom.ng),
+                                          f.dom.pitch * sizeof(double),
+                                          init + n * nc + (int64_t)p.jlo * f.L.nx + p.ilo, f.L.nx * sizeof(double),
+                                          p.nx * sizeof(double), p.ny, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                        return HF_ERR_CUDA;
+                continue;
+            }
             const int32_t reg[4] = {p.ilo, p.jlo, p.ilo + p.nx - 1, p.jlo + p.ny - 1};
             r = hf_interp_coarse_to_fine(m->ctx, &c.dom, c.U, &p, f.U, reg, s);
             if (r != HF_OK) return r;
@@ -662,6 +677,8 @@ hf_status hf_amr_regrid(hf_amr* m, void* stream) {
     if (r == HF_OK) r = totals(m, after, s);
     if (r != HF_OK) return r;
     ++m->regrids;
+    // building the hierarchy from given level states is InitFromScratch, not a remap
+    if (!m->init.empty()) return HF_OK;
     // regridChecked (:369-371): the conserved totals must survive the remap (relative to
     // the total of the magnitudes, so that a component summing to ~0 is judged fairly)
     for (int n = 0; n < m->nv; ++n)
@@ -671,7 +688,14 @@ hf_status hf_amr_regrid(hf_amr* m, void* stream) {
 
 hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, const hf_amr_opts* o, hf_amr** out,
                         void* stream) {
+    return hf_amr_create_levels(ctx, base, &U0, 1, o, out, stream);
+}
+
+hf_status hf_amr_create_levels(hf_ctx* ctx, const hf_level* base, const double* const* U_levels, int nlevels,
+                               const hf_amr_opts* o, hf_amr** out, void* stream) {
     if (out) *out = nullptr;
+    if (!U_levels || nlevels < 1 || !o || nlevels > o->max_level + 1) return HF_ERR_ARG;
+    const double* U0 = U_levels[0];
     if (!ctx || !base || !U0 || !o || !out || o->max_level < 0 || o->max_level > 6 || o->block < 8 ||
         (o->block & 1) || base->nx % (o->block / 2) || base->ny % (o->block / 2) || o->tag_buffer < 0 ||
         !(o->rtol > 0) || !(o->atol > 0))
@@ -738,8 +762,17 @@ hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, con
                                    a.L.nx * sizeof(double), a.L.ny, cudaMemcpyDeviceToDevice, s) == cudaSuccess;
     }
     hf_status r = ok ? rebuild(m, s) : HF_ERR_CUDA;
-    // initial hierarchy: one regrid per level
+    // initial hierarchy: one regrid per level (new blocks from the given level states)
+    m->init.assign(U_levels, U_levels + nlevels);
     for (int k = 0; r == HF_OK && k < o->max_level; ++k) r = hf_amr_regrid(m, stream);
+    if (r == HF_OK && nlevels > 1) {
+        // run() (:401): average(state) after InitFromScratch, then validate(state)
+        double* U[8];
+        arrays(m, [](AmrLevel& a) { return a.U; }, U);
+        r = average_all(m, U, s);
+        if (r == HF_OK) r = validate_all(m, U, s);
+    }
+    m->init.clear();
     m->regrids = 0;
     if (r != HF_OK) {
         hf_amr_destroy(m);

@@ -218,15 +218,18 @@ def write_amr_boxes(path, boxes, base):
 
 def run_amr_case(ctx, level, U0, end_time, out_dir, cfl=0.5, output_times=None, max_level=1, block=32,
                  tag_buffer=2, regrid_interval=8, chemistry=True, chem="batched", tags=None, max_steps=10 ** 7,
-                 stepper=None, props=None):
+                 stepper=None, props=None, U_levels=None):
     """BlockAMR::run (BlockAMR.cpp:400-439) on the block-AMR stepper, writing the
     reference's files: state_N.csv and boxes_N.csv at t = 0 and at every output time
     (leaf cells of every level), history.csv after every step, summary.json.  The step is
     the CFL step of all levels shortened to land on the next output time; a regrid
     follows every regrid_interval-th step unless it reached the end time (:420).
-    stepper / props: an object with AmrStepper's methods built with regrid_interval 0,
-    and props(q (NV, n) numpy) -> (p, T) numpy, in place of the GPU stepper and the GPU
-    EOS (the host logic is the same for any hierarchy).  Returns the summary dict."""
+    U_levels: the initial state of levels 1, 2, ... (case.levels), taken by the initial
+    hierarchy's new blocks as the reference's MakeNewLevelFromScratch does; without it
+    they interpolate level 0.  stepper / props: an object with AmrStepper's methods built
+    with regrid_interval 0, and props(q (NV, n) numpy) -> (p, T) numpy, in place of the GPU
+    stepper and the GPU EOS (the host logic is the same for any hierarchy).  Returns the
+    summary dict."""
     os.makedirs(out_dir, exist_ok=True)
     targets = list(output_times or [end_time])
     prev = 0.0
@@ -237,7 +240,8 @@ def run_amr_case(ctx, level, U0, end_time, out_dir, cfl=0.5, output_times=None, 
     if abs(targets[-1] - end_time) > 1e-14 * end_time:
         raise ValueError("last output must equal final time")
     am = stepper or S.AmrStepper(ctx, level, U0, max_level=max_level, block=block, tag_buffer=tag_buffer,
-                                 regrid_interval=0, chemistry=chemistry, chem=chem, rtol=1e-8, atol=1e-15, tags=tags)
+                                 regrid_interval=0, chemistry=chemistry, chem=chem, rtol=1e-8, atol=1e-15, tags=tags,
+                                 U_levels=U_levels)
     ns = U0.shape[0] - 3
 
     def gpu_props(q):

@@ -657,10 +657,12 @@ class AmrStepper:
     blocks of `block` cells, no time subcycling, regrid every `regrid_interval` steps.
 
     level: the base level (make_level); U0: (NV, ny, nx) float64 CUDA tensor; tags: keyword
-    arguments of tag_criteria (ErrorEst keys, density_tag extension)."""
+    arguments of tag_criteria (ErrorEst keys, density_tag extension); U_levels: the initial
+    state of levels 1, 2, ... ((NV, ny_l, nx_l) CUDA tensors or None), which the initial
+    hierarchy takes for its new blocks instead of interpolating (hf_amr_create_levels)."""
 
     def __init__(self, ctx, level, U0, max_level=1, block=32, tag_buffer=2, regrid_interval=0, chemistry=True,
-                 chem="batched", rtol=1e-8, atol=1e-15, tags=None):
+                 chem="batched", rtol=1e-8, atol=1e-15, tags=None, U_levels=None):
         _need_state(ctx, U0, "U0")
         self.ctx = ctx
         o = L.AmrOpts()
@@ -674,8 +676,20 @@ class AmrStepper:
         self.nv = U0.shape[0]
         h = ctypes.c_void_p()
         torch.cuda.synchronize()
-        ctx.check(ctx.lib.hf_amr_create(ctx.h, ctypes.byref(level), _ptr(U0.contiguous()), ctypes.byref(o),
-                                        ctypes.byref(h), _stream()), "amr_create")
+        if U_levels:
+            keep = [U0.contiguous()] + [None if u is None else u.contiguous() for u in U_levels]
+            for lev, u in enumerate(keep[1:], 1):
+                if u is not None:
+                    _need_state(ctx, u, "U_levels")
+                    if tuple(u.shape[1:]) != (level.ny << lev, level.nx << lev):
+                        raise ValueError("U_levels[%d] must cover level %d" % (lev - 1, lev))
+            ptrs = (ctypes.c_void_p * len(keep))(*[None if u is None else u.data_ptr() for u in keep])
+            ctx.check(ctx.lib.hf_amr_create_levels(ctx.h, ctypes.byref(level), ptrs, len(keep), ctypes.byref(o),
+                                                   ctypes.byref(h), _stream()), "amr_create_levels")
+            torch.cuda.synchronize()
+        else:
+            ctx.check(ctx.lib.hf_amr_create(ctx.h, ctypes.byref(level), _ptr(U0.contiguous()), ctypes.byref(o),
+                                            ctypes.byref(h), _stream()), "amr_create")
         self.h = h
 
     def close(self):

@@ -362,6 +362,15 @@ typedef struct hf_amr hf_amr;
 /* U0: level-0 state, SoA [NV][ny][nx] device memory (copied). */
 HF_EXPORT hf_status hf_amr_create(hf_ctx* ctx, const hf_level* base, const double* U0, const hf_amr_opts* opts,
                                   hf_amr** out, void* stream);
+/* As hf_amr_create, with the initial state of levels 0..nlevels-1 (host array of device
+ * pointers to SoA [NV][ny_l][nx_l] dense level states; entries after the first may be
+ * NULL): while the initial hierarchy is built, a block of level l that becomes active
+ * takes U_levels[l] instead of the interpolation of level l-1 (the reference's
+ * MakeNewLevelFromScratch, BlockAMR.cpp:124-131, evaluates the initial condition on
+ * every level), the remap check is skipped, and the levels are then averaged down and
+ * validated (run(), :401).  nlevels <= max_level + 1. */
+HF_EXPORT hf_status hf_amr_create_levels(hf_ctx* ctx, const hf_level* base, const double* const* U_levels,
+                                         int nlevels, const hf_amr_opts* opts, hf_amr** out, void* stream);
 HF_EXPORT void hf_amr_destroy(hf_amr* amr);
 /* One Strang step of every level; *dt as hf_stepper_step (<= 0: stableDt over all levels). */
 HF_EXPORT hf_status hf_amr_step(hf_amr* amr, double cfl, double* dt, void* stream);

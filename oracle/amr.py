@@ -108,18 +108,27 @@ class Hierarchy:
         self.chemistry, self.rtol, self.atol = chemistry, rtol, atol
         self.crit, self.buf, self.interval = crit, tag_buffer, regrid_interval
         self.time, self.steps, self.regrids, self.retries = 0.0, 0, 0, 0
+        self._init = []
         self.first_order_stages, self.roundoff_repairs = 0, 0
         self._rebuild()
         self.X = self.average_all(self.X)
 
     @classmethod
-    def from_base(cls, U0, domain, block, crit, max_level=1, tag_buffer=1, regrid_interval=0, **kw):
-        """The hierarchy the GPU stepper builds from the base level alone (hf_amr_create):
-        level 0 = U0, then one regrid per level."""
+    def from_base(cls, U0, domain, block, crit, max_level=1, tag_buffer=1, regrid_interval=0, levels=None, **kw):
+        """The hierarchy the GPU stepper builds from the base level (hf_amr_create): level
+        0 = U0, then one regrid per level.  levels: the initial state of levels 1, 2, ...
+        ((ny_l, nx_l, NV) or None; hf_amr_create_levels): a new block takes it instead of
+        the interpolation, the remap check is skipped, and the levels are then averaged
+        down and validated (MakeNewLevelFromScratch, BlockAMR.cpp:124-131; run(), :401)."""
         o = cls([U0], [None], domain, block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval,
                 max_level=max_level, **kw)
+        o._init = [None] + list(levels or [])
         for _ in range(max_level):
             o.regrid()
+        if levels:
+            o.X = o.average_all(o.X)
+            o._check(o.X, "the initial hierarchy")
+        o._init = []
         o.regrids = 0
         return o
 
@@ -414,8 +423,13 @@ class Hierarchy:
         anyb = bool(nxt.any())
         self.finest = max(self.finest, l + 1) if anyb else l
         f = self.X[l + 1]
+        init = self._init[l + 1] if l + 1 < len(self._init) else None
         for bj, bi in zip(*np.nonzero(nxt)):
             if had and prev[bj, bi]:
+                continue
+            if init is not None:
+                f[2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B] = init[bj * B:(bj + 1) * B,
+                                                                               bi * B:(bi + 1) * B]
                 continue
             for fj in range(bj * B, (bj + 1) * B):
                 for fi in range(bi * B, (bi + 1) * B):
@@ -432,6 +446,8 @@ class Hierarchy:
             self._regrid_level(l)
             l += 1
         self.regrids += 1
+        if self._init:
+            return  # building the hierarchy from given level states is not a remap
         after = self.totals()
         if np.any(np.abs(after - before) > 1e-8 * scale):
             raise RuntimeError("regridChecked: the totals changed in the remap")

@@ -386,3 +386,33 @@ def test_flux_adjoint_matches_oracle_fd(gpu, oracle):
     got, want = np.array(got), np.array(want)
     assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
     assert np.all(np.abs(got - want) <= 1e-4 * np.maximum(np.abs(want), 1.0))
+
+
+def test_reference_blast_config_through_the_amr_stepper(gpu, oracle, tmp_path):
+    """The reference's reacting blast check (tests/validate.py:174-191) on the block-AMR
+    stepper through case.load / case.levels and run_amr_case, the fine level built from
+    the initial condition at its resolution (hf_amr_create_levels): two steps of 1e-7 s
+    without a retry, mass and energy within 1e-11, and the recorded peak
+    Y_H + Y_O + Y_OH 1.4893699370443747e-07 within 5e-6 relative (docs/amr_checks.json:101)."""
+    import json
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import case, output
+    from test_output_amr import check_geometry
+    c = dict(problem="blast2d", base_cells=[16, 16], length=[.01, .01], max_level=1, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="physics", periodic=[0, 0], chemistry=True, cfl=.6,
+             end_time=2e-7, output_times=[1e-7, 2e-7], regrid_interval=2, center=[.005, .005], radius=.0015,
+             boundary_hi=["reflecting", "reflecting"])
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    s = output.run_amr_case(gpu, hf.make_level(**lvd), cuda(U0), run["end_time"], str(tmp_path), cfl=run["cfl"],
+                            output_times=run["output_times"], max_level=run["max_level"], block=run["block"],
+                            tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"], chemistry=True,
+                            tags=run["tags"], U_levels=[cuda(u) for u in lv[1:]])
+    assert s["steps"] == 2 and s["retries"] == 0
+    data = np.genfromtxt(tmp_path / "state_2.csv", names=True, delimiter=",")
+    check_geometry(data, (16, 16), (.01, .01), int(data["level"].max()))
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+    peak = float(np.max(data["Y_H"] + data["Y_O"] + data["Y_OH"]))
+    assert abs(peak / H.reference_records()["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6

@@ -98,10 +98,10 @@ def test_state_rows_of_the_oracle_hierarchy(oracle, out, tmp_path):
 class OracleAmr:
     """AmrStepper's interface over the composite oracle (regrids driven by the caller)."""
 
-    def __init__(self, oracle, amr, U0, lvd, block, crit, max_level, tag_buffer):
+    def __init__(self, oracle, amr, U0, lvd, block, crit, max_level, tag_buffer, chemistry=False, levels=None):
         self.o, self.B = oracle, block
         self.h = amr.Hierarchy.from_base(U0, lvd, block, crit, max_level=max_level, tag_buffer=tag_buffer,
-                                         regrid_interval=0, chemistry=False)
+                                         regrid_interval=0, chemistry=chemistry, levels=levels)
 
     def info(self, lev):
         h = self.h
@@ -183,3 +183,38 @@ def test_run_amr_case_host_logic(oracle, out, tmp_path):
     hist = np.genfromtxt(tmp_path / "history.csv", names=True, delimiter=",")
     assert len(hist) == steps + 1 and hist["regrids"][-1] == s["regrids"] and hist["finest_level"][-1] == 2
     assert abs(hist["t"][-1] - end) == 0 and np.all(np.diff(hist["t"]) > 0)
+
+
+def test_reference_blast_config_through_the_amr_runner(oracle, out, tmp_path):
+    """The reference's reacting blast check (tests/validate.py:174-191: config, then the
+    peak Y_H + Y_O + Y_OH of the last state file) through case.load / case.levels and
+    run_amr_case, with the composite oracle standing in for the GPU stepper: two steps of
+    1e-7 s without a retry, and the recorded peak 1.4893699370443747e-07 within 5e-6
+    relative (docs/amr_checks.json:101)."""
+    import amr
+    import torch
+    from hyperflow_gb300 import case, solver as S
+    c = dict(problem="blast2d", base_cells=[16, 16], length=[.01, .01], max_level=1, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="physics", periodic=[0, 0], chemistry=True, cfl=.6,
+             end_time=2e-7, output_times=[1e-7, 2e-7], regrid_interval=2, center=[.005, .005], radius=.0015,
+             boundary_hi=["reflecting", "reflecting"])
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    crit = amr.criteria(chemistry=run["chemistry"], **run["tags"])
+    stepper = OracleAmr(oracle, amr, U0.transpose(1, 2, 0), lvd, run["block"], crit, run["max_level"], run["tag_buffer"],
+                        chemistry=True, levels=[u.transpose(1, 2, 0) for u in lv[1:]])
+
+    def props(q):
+        p, _, T, st = oracle.properties(np.ascontiguousarray(q.T))
+        assert not np.any(st)
+        return p, T
+
+    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+                         cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
+                         block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
+                         chemistry=True, stepper=stepper, props=props)
+    assert s["steps"] == 2 and s["retries"] == 0 and s["regrids"] == 0
+    data = np.genfromtxt(tmp_path / "state_2.csv", names=True, delimiter=",")
+    check_geometry(data, (16, 16), (.01, .01), int(data["level"].max()))
+    peak = float(np.max(data["Y_H"] + data["Y_O"] + data["Y_OH"]))
+    assert abs(peak / H.reference_records()["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6
