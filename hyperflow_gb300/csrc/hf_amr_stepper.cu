@@ -763,7 +763,7 @@ hf_status hf_amr_create_levels(hf_ctx* ctx, const hf_level* base, const double* 
     }
     hf_status r = ok ? rebuild(m, s) : HF_ERR_CUDA;
     // initial hierarchy: one regrid per level (new blocks from the given level states)
-    m->init.assign(U_levels, U_levels + nlevels);
+    if (nlevels > 1) m->init.assign(U_levels, U_levels + nlevels);
     for (int k = 0; r == HF_OK && k < o->max_level; ++k) r = hf_amr_regrid(m, stream);
     if (r == HF_OK && nlevels > 1) {
         // run() (:401): average(state) after InitFromScratch, then validate(state)
