@@ -122,7 +122,7 @@ class Hierarchy:
         down and validated (MakeNewLevelFromScratch, BlockAMR.cpp:124-131; run(), :401)."""
         o = cls([U0], [None], domain, block, crit=crit, tag_buffer=tag_buffer, regrid_interval=regrid_interval,
                 max_level=max_level, **kw)
-        o._init = [None] + list(levels or [])
+        o._init = [None] + list(levels) if levels else []
         for _ in range(max_level):
             o.regrid()
         if levels:
