@@ -16,6 +16,9 @@ FIELDS = {
                                               "energy_relative_change"],
     ("case_checks.json", "cases", "teng_case1"): ["final_time_s", "steps", "retries", "dx_min_m", "dy_min_m"],
     ("amr_checks.json", "tests", "moving_refine_coarsen"): ["steps"],
+    ("amr_checks.json", "tests", "uniform_local_amr"): ["leaf_cells"],
+    ("amr_checks.json", "tests", "zero_dimensional_cvode"): ["chemistry_cell_calls", "expected_leaf_calls",
+                                                             "relative_temperature_error", "max_absolute_Y_error"],
     ("amr_checks.json", "tests", "blast2d_inert"): ["steps", "transpose_pressure_error"],
     ("amr_checks.json", "tests", "blast2d_reacting"): ["peak_radical_mass_fraction", "steps", "retries",
                                                        "first_order_stages"],

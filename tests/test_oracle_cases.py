@@ -5,7 +5,8 @@ outcomes the reference records for them (tests/golden/reference_records.json):
   checks of HyperFlow_V3/tests/check_cases.py:43-48,58,68.
 - HyperFlow_V3/docs/amr_checks.json:35,52,101: the moving entropy wave takes 58 steps to
   4e-6 s, the inert blast 37 steps to 2e-6 s, and the reacting blast ends with a peak
-  Y_H + Y_O + Y_OH of 1.4893699370443747e-07.
+  Y_H + Y_O + Y_OH of 1.4893699370443747e-07; the uniform chemistry run makes 5824
+  chemistry cell calls over 1456 leaf cells, 4 steps.
 
 The reference ran both cases on its AMR hierarchy.  Here each case is one level at the
 finest resolution.  The step is the CFL step of the largest wave rate over all levels
@@ -129,3 +130,20 @@ def test_entropy_wave_check(oracle, W):
     final_checks(oracle, F)
     a, b = U.transpose(1, 2, 0).reshape(-1, 12).sum(0), F.reshape(-1, 12).sum(0)
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+
+
+def test_uniform_chemistry_check(oracle):
+    """validate.py:140-158 (the uniform-chemistry run of the BASE config at 1500 K / 5 atm
+    to 2e-7 s) on its finest level: the reference records 5824 chemistry cell calls over
+    1456 leaf cells (docs/amr_checks.json), i.e. 4 steps; the oracle takes 4 CFL steps."""
+    from hyperflow_gb300 import case
+    c = dict(problem="uniform", base_cells=[16, 16], length=[.01, .01], max_level=2, periodic=[1, 1],
+             chemistry=True, cfl=.6, end_time=2e-7, T0=1500., P0=5 * 101325.)
+    U, lvd, run_opts = case.load(c, refine=2)
+    F, dts, rollbacks = run(oracle, U, lvd, dict(run_opts, chemistry=True))
+    rec = REC["zero_dimensional_cvode"]
+    assert rec["chemistry_cell_calls"] == rec["expected_leaf_calls"]
+    assert len(dts) == rec["chemistry_cell_calls"] // REC["uniform_local_amr"]["leaf_cells"] and rollbacks == 0
+    final_checks(oracle, F)
+    T = oracle.properties(F.reshape(-1, 12))[2]
+    assert np.ptp(T) == 0.0  # a uniform state stays uniform (validate.py:95-97)
