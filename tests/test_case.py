@@ -95,3 +95,36 @@ def test_rejections():
         case.load(dict(BASE, cfl=0.9))
     with pytest.raises(ValueError):
         case.load(dict(BASE, problem="teng_osw", inflow_speed=2000.0, wedge_angle_deg=95.0))
+
+
+@pytest.mark.parametrize("problem", ["uniform", "sod_x", "sod_y", "example6", "example7", "entropy_wave", "blast2d"])
+def test_every_problem_loads_admissible_states(oracle, problem):
+    """Every initial condition of BlockAMR::initial (BlockAMR.cpp:84-121) on a small grid:
+    admissible cells, and the shape of each problem's initial field."""
+    from hyperflow_gb300 import case
+    c = dict(problem=problem, base_cells=[16, 8], length=[1.0, 0.5] if problem.startswith("example") else [.01, .005],
+             end_time=1e-7)
+    U, lv, run = case.load(c)
+    q = U.reshape(12, -1).T
+    p, _, T, st = oracle.properties(np.ascontiguousarray(q))
+    assert not np.any(st)
+    fresh, hot = case.states(c)
+    if problem == "uniform":
+        assert np.all(U == fresh[:, None, None])
+    elif problem == "sod_x":       # hot left of the interface at x = L/2, fresh right of it
+        assert np.allclose(U[:, :, :8], hot[:, None, None], rtol=1e-12, atol=0)
+        assert np.allclose(U[:, :, 8:], fresh[:, None, None], rtol=1e-12, atol=0)
+    elif problem == "sod_y":       # (the cell fractions at the interface round to 1 +- 1 ulp)
+        assert np.allclose(U[:, :4, :], hot[:, None, None], rtol=1e-12, atol=0)
+        assert np.allclose(U[:, 4:, :], fresh[:, None, None], rtol=1e-12, atol=0)
+    elif problem == "example6":    # hot (moving at 800 m/s) up to x = 0.4
+        rho = U[:9].sum(0)
+        assert np.allclose(U[9, :, :6] / rho[:, :6], 800.0) and np.all(U[9, :, 7:] == 0.0)
+    elif problem == "example7":    # the hot front is furthest right in the middle rows
+        hot_cols = (U[9] != 0).sum(1)
+        assert hot_cols[3] >= hot_cols[0] and hot_cols.min() >= 8
+    elif problem == "entropy_wave":  # the temperature dip is centred at (0.3 L, 0.5 H)
+        j, i = np.unravel_index(np.argmin(T.reshape(8, 16)), (8, 16))
+        assert (j, i) in ((3, 4), (4, 4), (3, 5), (4, 5))
+    else:                          # the hot disc at (0.3 L, 0.5 H), radius 0.1 H
+        assert T.max() > 1000.0 and T.reshape(8, 16)[0, -1] == pytest.approx(300.0, rel=1e-12)
