@@ -120,7 +120,7 @@ def test_every_problem_loads_admissible_states(oracle, problem):
     elif problem == "example6":    # hot (moving at 800 m/s) up to x = 0.4
         rho = U[:9].sum(0)
         assert np.allclose(U[9, :, :6] / rho[:, :6], 800.0) and np.all(U[9, :, 7:] == 0.0)
-    elif problem == "example7":    # the hot front is furthest right in the middle rows
+    elif problem == "example7":    # hot (2000 m/s) left of x = max(0.5, 0.25 + distance to a wall)
         hot_cols = (U[9] != 0).sum(1)
         assert hot_cols[3] >= hot_cols[0] and hot_cols.min() >= 8
     elif problem == "entropy_wave":  # the temperature dip is centred at (0.3 L, 0.5 H)
