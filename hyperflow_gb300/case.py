@@ -122,15 +122,18 @@ def load(c, refine=0):
                chemistry=bool(c.get("chemistry", True)), max_level=c.get("max_level", 2),
                tag_buffer=c.get("tag_buffer", 2),
                regrid_interval=c.get("regrid_interval", 8) if c.get("adaptive", True) else 0, tags=tags,
-               block=block_size(nc, c.get("max_grid_size", 32)))
+               block=block_size(nc, c.get("blocking_factor", 4), c.get("max_grid_size", 32)))
     return U, level, run
 
 
-def block_size(base_cells, max_grid_size=32):
-    """The largest even block of at most max_grid_size cells (and at least 8) that the
-    block-AMR stepper can lay on this base grid (base cells divisible by half a block),
-    or None."""
-    for b in range(int(max_grid_size) // 2 * 2, 7, -2):
+def block_size(base_cells, blocking_factor=4, max_grid_size=32):
+    """The block of the block-AMR stepper closest to the reference's refinement
+    granularity: the smallest even size of at least max(8, blocking_factor) cells and at
+    most max_grid_size that tiles the refined levels (base cells divisible by half a
+    block), or None.  (Larger blocks refine coarser regions: on the reference's inert
+    blast check, blocks of 16 leave the finest level empty at the start.)"""
+    lo = max(8, int(blocking_factor) + (int(blocking_factor) & 1))
+    for b in range(lo, int(max_grid_size) + 1, 2):
         if base_cells[0] % (b // 2) == 0 and base_cells[1] % (b // 2) == 0:
             return b
     return None

@@ -51,7 +51,7 @@ def test_teng_case1_smoke_case(cases):
     assert np.array_equal(U, Uw)
     same_level(lv, lw)
     assert run["cfl"] == cw["cfl"] and run["end_time"] == cw["end_time"]
-    assert run["block"] == 32 and run["tags"]["temperature_tag"] == 0.06
+    assert run["block"] == 8 and run["tags"]["temperature_tag"] == 0.06
 
 
 @pytest.mark.parametrize("reacting", [False, True])
@@ -84,7 +84,7 @@ def test_moving_refinement_check():
     Uw, lw, cw = W.entropy_wave()
     assert np.allclose(U, Uw, rtol=1e-14, atol=0)
     assert lv["periodic"] == (1, 1) and lv["nx"] == 64 and lv["dx"] == lw["dx"]
-    assert run["tags"]["box_only"] and run["tags"]["velocity"] == (300.0, 200.0) and run["block"] == 16
+    assert run["tags"]["box_only"] and run["tags"]["velocity"] == (300.0, 200.0) and run["block"] == 8
 
 
 def test_rejections():

@@ -416,3 +416,32 @@ def test_reference_blast_config_through_the_amr_stepper(gpu, oracle, tmp_path):
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
     peak = float(np.max(data["Y_H"] + data["Y_O"] + data["Y_OH"]))
     assert abs(peak / H.reference_records()["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6
+
+
+def test_reference_inert_blast_config_through_the_amr_stepper(gpu, tmp_path):
+    """The reference's inert blast check (tests/validate.py:122-137) on three levels of the
+    block-AMR stepper through case.load / case.levels and run_amr_case: 37 steps to
+    2e-6 s as recorded (docs/amr_checks.json:52), no retry, leaf cells tiling the domain,
+    mass and energy within 1e-11."""
+    import json
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import case, output
+    from test_output_amr import check_geometry
+    c = dict(problem="blast2d", base_cells=[24, 24], length=[.02, .02], max_level=2, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="physics", periodic=[0, 0], chemistry=False, cfl=.6,
+             end_time=2e-6, output_times=[1e-6, 2e-6], regrid_interval=4, center=[.01, .01], radius=.002,
+             boundary_lo=["reflecting", "reflecting"], boundary_hi=["reflecting", "reflecting"], pressure_tag=.06,
+             temperature_tag=.06)
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    s = output.run_amr_case(gpu, hf.make_level(**lvd), cuda(U0), run["end_time"], str(tmp_path), cfl=run["cfl"],
+                            output_times=run["output_times"], max_level=run["max_level"], block=run["block"],
+                            tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"], chemistry=False,
+                            tags=run["tags"], U_levels=[cuda(u) for u in lv[1:]])
+    assert s["steps"] == H.reference_records()["blast2d_inert"]["steps"] and s["retries"] == 0
+    for k in range(3):
+        data = np.genfromtxt(tmp_path / ("state_%d.csv" % k), names=True, delimiter=",")
+        check_geometry(data, (24, 24), (.02, .02), int(data["level"].max()))
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11

@@ -218,3 +218,42 @@ def test_reference_blast_config_through_the_amr_runner(oracle, out, tmp_path):
     check_geometry(data, (16, 16), (.01, .01), int(data["level"].max()))
     peak = float(np.max(data["Y_H"] + data["Y_O"] + data["Y_OH"]))
     assert abs(peak / H.reference_records()["blast2d_reacting"]["peak_radical_mass_fraction"] - 1) < 5e-6
+
+
+def test_reference_inert_blast_config_through_the_amr_runner(oracle, out, tmp_path):
+    """The reference's inert blast check (tests/validate.py:122-137) on three levels
+    through case.load / case.levels and run_amr_case, the composite oracle standing in
+    for the GPU stepper: 37 steps to 2e-6 s as recorded (docs/amr_checks.json:52), no
+    retry, leaf cells tiling the domain, mass and energy within 1e-11."""
+    import json
+    import amr
+    import torch
+    from hyperflow_gb300 import case, solver as S
+    c = dict(problem="blast2d", base_cells=[24, 24], length=[.02, .02], max_level=2, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="physics", periodic=[0, 0], chemistry=False, cfl=.6,
+             end_time=2e-6, output_times=[1e-6, 2e-6], regrid_interval=4, center=[.01, .01], radius=.002,
+             boundary_lo=["reflecting", "reflecting"], boundary_hi=["reflecting", "reflecting"], pressure_tag=.06,
+             temperature_tag=.06)
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    crit = amr.criteria(chemistry=False, **run["tags"])
+    stepper = OracleAmr(oracle, amr, U0.transpose(1, 2, 0), lvd, run["block"], crit, run["max_level"],
+                        run["tag_buffer"], levels=[u.transpose(1, 2, 0) for u in lv[1:]])
+
+    def props(q):
+        p, _, T, st = oracle.properties(np.ascontiguousarray(q.T))
+        assert not np.any(st)
+        return p, T
+
+    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+                         cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
+                         block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
+                         chemistry=False, stepper=stepper, props=props)
+    assert s["steps"] == H.reference_records()["blast2d_inert"]["steps"] and s["retries"] == 0
+    assert s["finest_level"] == 2
+    for k in range(3):
+        data = np.genfromtxt(tmp_path / ("state_%d.csv" % k), names=True, delimiter=",")
+        check_geometry(data, (24, 24), (.02, .02), int(data["level"].max()))
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
