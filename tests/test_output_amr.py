@@ -257,3 +257,41 @@ def test_reference_inert_blast_config_through_the_amr_runner(oracle, out, tmp_pa
     summ = json.loads((tmp_path / "summary.json").read_text())
     a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+
+
+def test_reference_moving_refinement_config_through_the_amr_runner(oracle, out, tmp_path):
+    """The reference's moving-refinement check (tests/validate.py:104-119: the entropy wave
+    with box tags moving at (300, 200) m/s, three levels, a regrid every 4 steps) through
+    case.load / case.levels and run_amr_case over the composite oracle: 58 steps to 4e-6 s
+    as recorded (docs/amr_checks.json:35), no retry, refinement both gained and lost,
+    mass and energy within 1e-11 on the periodic box."""
+    import json
+    import amr
+    import torch
+    from hyperflow_gb300 import case, solver as S
+    c = dict(problem="entropy_wave", base_cells=[16, 16], length=[.01, .01], max_level=2, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="box", tag_box=[.002, .004, .003, .005], periodic=[1, 1],
+             chemistry=False, cfl=.6, end_time=4e-6, output_times=[2e-6, 4e-6], regrid_interval=4,
+             center=[.003, .004], sigma=.0007, tag_velocity=[300., 200.], u0=300., v0=200.)
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    stepper = OracleAmr(oracle, amr, U0.transpose(1, 2, 0), lvd, run["block"],
+                        amr.criteria(chemistry=False, **run["tags"]), run["max_level"], run["tag_buffer"],
+                        levels=[u.transpose(1, 2, 0) for u in lv[1:]])
+    first = stepper.h.acts[2].copy()
+
+    def props(q):
+        p, _, T, st = oracle.properties(np.ascontiguousarray(q.T))
+        assert not np.any(st)
+        return p, T
+
+    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+                         cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
+                         block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
+                         chemistry=False, stepper=stepper, props=props)
+    assert s["steps"] == H.reference_records()["moving_refine_coarsen"]["steps"] and s["retries"] == 0
+    last = stepper.h.acts[2]
+    assert np.any(last & (1 - first)) and np.any(first & (1 - last))
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
