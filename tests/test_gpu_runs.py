@@ -445,3 +445,27 @@ def test_reference_inert_blast_config_through_the_amr_stepper(gpu, tmp_path):
     summ = json.loads((tmp_path / "summary.json").read_text())
     a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+
+
+def test_reference_moving_refinement_config_through_the_amr_stepper(gpu, tmp_path):
+    """The reference's moving-refinement check (tests/validate.py:104-119) on three levels
+    of the block-AMR stepper through case.load / case.levels and run_amr_case: 58 steps
+    to 4e-6 s as recorded (docs/amr_checks.json:35), no retry, mass and energy within
+    1e-11 on the periodic box."""
+    import json
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import case, output
+    c = dict(problem="entropy_wave", base_cells=[16, 16], length=[.01, .01], max_level=2, blocking_factor=4,
+             max_grid_size=16, tag_buffer=1, tag_mode="box", tag_box=[.002, .004, .003, .005], periodic=[1, 1],
+             chemistry=False, cfl=.6, end_time=4e-6, output_times=[2e-6, 4e-6], regrid_interval=4,
+             center=[.003, .004], sigma=.0007, tag_velocity=[300., 200.], u0=300., v0=200.)
+    U0, lvd, run = case.load(c)
+    lv = case.levels(c)
+    s = output.run_amr_case(gpu, hf.make_level(**lvd), cuda(U0), run["end_time"], str(tmp_path), cfl=run["cfl"],
+                            output_times=run["output_times"], max_level=run["max_level"], block=run["block"],
+                            tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"], chemistry=False,
+                            tags=run["tags"], U_levels=[cuda(u) for u in lv[1:]])
+    assert s["steps"] == H.reference_records()["moving_refine_coarsen"]["steps"] and s["retries"] == 0
+    summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
