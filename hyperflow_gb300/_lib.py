@@ -118,6 +118,9 @@ SIGNATURES = [
     ("hf_cfl_dt", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d, _dp, _vp]),
     ("hf_validate", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp,
                            ctypes.POINTER(_i64), _vp]),
+    ("hf_repair_roundoff", _i32, [_vp, ctypes.c_int, ctypes.POINTER(Level), ctypes.POINTER(ctypes.POINTER(Patch)),
+                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                  ctypes.POINTER(_i64), _vp]),
     ("hf_stepper_create", _i32, [_vp, ctypes.POINTER(Level), _vp, ctypes.c_int, _d, _d, ctypes.c_int, ctypes.c_int,
                                  ctypes.POINTER(_vp)]),
     ("hf_stepper_destroy", None, [_vp]),

@@ -28,6 +28,7 @@ struct hf_ctx {
     int d_patch_cap = 0;
     int64_t* d_off = nullptr;  // per-patch offsets of the multi-patch flux launches
     int d_off_cap = 0;
+    RepairScratch* rep = nullptr;  // roundoff repair scratch (fixed size)
     // tensor-map cache for the fused flux kernel
     struct TMap { const double* base; hf_patch P; alignas(64) unsigned char map[128]; };
     std::vector<TMap> tmaps;
@@ -157,6 +158,10 @@ void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries) 
     ctx->cnt.first_order_stages += first_order_stages;
     ctx->cnt.retries += retries;
 }
+void ctx_add_repairs(hf_ctx* ctx, int64_t repairs) { ctx->cnt.roundoff_repairs += repairs; }
+void ctx_set_error(hf_ctx* ctx, const char* msg) {
+    if (ctx) ctx->err = msg;
+}
 void ctx_add_launches(hf_ctx* ctx, int64_t kernels, int64_t chem_cells, int64_t chem_steps) {
     ctx->cnt.kernel_launches += kernels;
     ctx->cnt.chem_cell_calls += chem_cells;
@@ -196,6 +201,7 @@ hf_status hf_init(const char* mechanism, int device, hf_ctx** out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->st, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->st_host, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->rep, repair_scratch_bytes());
     if (e == cudaSuccess) e = chem_set_rate_scale(nullptr);
     if (e == cudaSuccess) e = adjoint_set_rate_scale(nullptr);
     if (e != cudaSuccess) {
@@ -233,6 +239,7 @@ void hf_destroy(hf_ctx* ctx) {
     if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->d_patches) cudaFree(ctx->d_patches);
     if (ctx->d_off) cudaFree(ctx->d_off);
+    if (ctx->rep) cudaFree(ctx->rep);
     delete ctx;
 }
 
@@ -298,37 +305,88 @@ hf_status hf_interp_coarse_to_fine(hf_ctx* ctx, const hf_patch* coarse, const do
     return HF_OK;
 }
 
-// Roundoff repair + validation of one level after a stage (BlockAMR.cpp:257, 299-334).
+static char* aux_scratch(hf_ctx* ctx, size_t bytes);
+
+// Roundoff repair (the composite kernels over one level, every cell a leaf) + validation
+// of one level after a stage (BlockAMR.cpp:257, 299-334).
 static hf_status repair_and_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch, double* U,
                                      cudaStream_t s, int64_t* bad_cell) {
-    const double vol = level->dx * level->dy;
-    HF_CUDA(reset_status(ctx, s));
-    int64_t base = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-        base = 0;
-        for (int p = 0; p < npatch; ++p) {
-            HF_CUDA(launch_repair_scan(ctx->ns, patches[p], U, base, pass, ctx->st, s, &ctx->cnt.kernel_launches));
-            base += (int64_t)patches[p].nx * patches[p].ny;
-        }
+    std::vector<int64_t> base(npatch);
+    int64_t b = 0, mc = 1;
+    for (int p = 0; p < npatch; ++p) {
+        base[p] = b;
+        b += (int64_t)patches[p].nx * patches[p].ny;
+        mc = std::max<int64_t>(mc, (int64_t)patches[p].nx * patches[p].ny);
     }
-    for (int p = 0; p < npatch; ++p)
-        HF_CUDA(launch_repair_apply(ctx->ns, patches[p], U, vol, ctx->st, s, &ctx->cnt.kernel_launches));
     HF_CUDA(upload_patches(ctx, patches, npatch, s));
-    HF_CUDA(launch_donor_fix(ctx->ns, ctx->d_patches, npatch, U, vol, ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(upload_offsets(ctx, base.data(), npatch, s));
+    RepairLevels R{};
+    R.nlev = 1;
+    R.lev[0] = RepairLevel{ctx->d_patches, ctx->d_off, nullptr, U, npatch, mc, level->dx * level->dy};
+    HF_CUDA(reset_status(ctx, s));
+    HF_CUDA(launch_composite_repair(ctx->ns, R, ctx->rep, ctx->st, s, &ctx->cnt.kernel_launches));
     HF_CUDA(read_status(ctx, s));
     if (ctx->st_host->flags & ST_MATERIAL) return fail(ctx, HF_ERR_NEGATIVE, "materially negative species after a stage");
     ctx->cnt.roundoff_repairs += (int64_t)ctx->st_host->repairs;
     HF_CUDA(reset_status(ctx, s));
-    base = 0;
+    int64_t vb = 0;
     for (int p = 0; p < npatch; ++p) {
-        HF_CUDA(launch_validate(ctx->ns, patches[p], U, base, ctx->st, s, &ctx->cnt.kernel_launches));
-        base += (int64_t)patches[p].nx * patches[p].ny;
+        HF_CUDA(launch_validate(ctx->ns, patches[p], U, vb, ctx->st, s, &ctx->cnt.kernel_launches));
+        vb += (int64_t)patches[p].nx * patches[p].ny;
     }
     HF_CUDA(read_status(ctx, s));
     if (ctx->st_host->flags) {
         if (bad_cell) *bad_cell = (int64_t)ctx->st_host->bad_cell;
         return fail(ctx, HF_ERR_INADMISSIBLE, "inadmissible state after a stage");
     }
+    return HF_OK;
+}
+
+hf_status hf_repair_roundoff(hf_ctx* ctx, int nlev, const hf_level* levels, const hf_patch* const* patches,
+                             const int* npatch, double* const* U, const uint8_t* const* leaf, int64_t* repairs,
+                             void* stream) {
+    if (repairs) *repairs = 0;
+    if (!ctx || nlev < 1 || nlev > REPAIR_MAX_LEVELS || !levels || !patches || !npatch || !U)
+        return fail(ctx, HF_ERR_ARG, "repair_roundoff: bad arguments");
+    for (int l = 0; l < nlev; ++l) {
+        if (!level_ok(levels[l]) || !patches[l] || npatch[l] <= 0 || !U[l])
+            return fail(ctx, HF_ERR_ARG, "repair_roundoff: bad level");
+        for (int p = 0; p < npatch[l]; ++p)
+            if (!patch_ok(patches[l][p])) return fail(ctx, HF_ERR_ARG, "repair_roundoff: bad patch");
+    }
+    const cudaStream_t s = S(stream);
+    // per-level device tables: patches | first-cell offsets, in the aux scratch
+    size_t bytes = 0;
+    for (int l = 0; l < nlev; ++l) bytes += ((sizeof(hf_patch) + sizeof(int64_t)) * (size_t)npatch[l] + 255) & ~size_t(255);
+    char* w = aux_scratch(ctx, bytes);
+    if (!w) return fail(ctx, HF_ERR_CUDA, "repair_roundoff: scratch allocation failed");
+    RepairLevels R{};
+    R.nlev = nlev;
+    size_t off = 0;
+    for (int l = 0; l < nlev; ++l) {
+        const int np = npatch[l];
+        std::vector<int64_t> base(np);
+        int64_t b = 0, mc = 1;
+        for (int p = 0; p < np; ++p) {
+            base[p] = b;
+            b += (int64_t)patches[l][p].nx * patches[l][p].ny;
+            mc = std::max<int64_t>(mc, (int64_t)patches[l][p].nx * patches[l][p].ny);
+        }
+        hf_patch* dp = reinterpret_cast<hf_patch*>(w + off);
+        int64_t* db = reinterpret_cast<int64_t*>(w + off + sizeof(hf_patch) * np);
+        off += ((sizeof(hf_patch) + sizeof(int64_t)) * (size_t)np + 255) & ~size_t(255);
+        HF_CUDA(cudaMemcpyAsync(dp, patches[l], sizeof(hf_patch) * np, cudaMemcpyHostToDevice, s));
+        HF_CUDA(cudaMemcpyAsync(db, base.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
+        HF_CUDA(cudaStreamSynchronize(s));
+        R.lev[l] = RepairLevel{dp, db, leaf ? leaf[l] : nullptr, U[l], np, mc, levels[l].dx * levels[l].dy};
+    }
+    HF_CUDA(reset_status(ctx, s));
+    HF_CUDA(launch_composite_repair(ctx->ns, R, ctx->rep, ctx->st, s, &ctx->cnt.kernel_launches));
+    HF_CUDA(read_status(ctx, s));
+    if (repairs) *repairs = (int64_t)ctx->st_host->repairs;
+    if (ctx->st_host->flags & ST_MATERIAL)
+        return fail(ctx, HF_ERR_NEGATIVE, "repair_roundoff: materially negative species or insufficient donor");
+    ctx->cnt.roundoff_repairs += (int64_t)ctx->st_host->repairs;
     return HF_OK;
 }
 

@@ -3,8 +3,11 @@
 //   average_down  BlockAMR.cpp:157-159 (AMReX average_down, ratio 2)
 //   reflux        BlockAMR.cpp:247-255 (FluxRegister CrseInit / FineAdd /
 //                 ClearInternalBorders / Reflux at scale 1)
+//   repair        BlockAMR.cpp:299-334 (repairRoundoff over the leaf cells of every level)
 // All reductions are deterministic: fixed partitions and fixed combination orders,
-// no floating-point atomics.
+// no floating-point atomics in a result (the repair's atomic deficit sum is only the
+// fallback past REPAIR_CAP negative entries).
+#include <cstddef>
 #include <cstring>
 #include "hf_internal.h"
 
@@ -219,6 +222,176 @@ cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_p
     k_reflux<<<dim3((unsigned)((mc + 127) / 128), (unsigned)ncoarse), 128, 0, s>>>(
         L, coarse_dev, cfx_off, cfy_off, fxc, fyc, Uc, fine_dev, ffx_off, ffy_off, fxf, fyf, cover, h, hdev, nv);
     *launches += 3;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- composite roundoff repair
+// repairRoundoff (BlockAMR.cpp:299-334) over the leaf cells of levels 0..nlev-1, in the
+// reference's order: levels in turn, the patches of a level in table order, the cells
+// of a patch row by row.  A cell is identified by its level and its patch-packed index
+// (base[p] + row-major index in patch p).
+//   scan pass 0: per species the peak partial density and the largest mass
+//                (value x cell volume) over all leaf cells;
+//   scan pass 1: donor = the first cell (lowest level, then lowest index) holding that
+//                mass (the reference keeps the first strictly larger mass);
+//   apply:       a negative value beyond 64 ulp of the peak, or a non-finite one, is
+//                material (the reference throws); smaller ones are zeroed and their
+//                deficits (-value x volume) recorded with the cell's key;
+//   fix:         one block sorts the recorded entries by (species, level, cell) and adds
+//                each species' deficits in that order, as the reference's loop does,
+//                then takes each deficit from its donor (material when the donor's mass
+//                does not exceed it).
+// Non-negative doubles order like their bit patterns, so maxima are integer atomics.
+__device__ __forceinline__ unsigned long long repair_key(int l, int64_t c) {
+    return ((unsigned long long)l << 52) | (unsigned long long)c;
+}
+
+template <int NS>
+__global__ void k_crep_scan(RepairLevel R, int l, int pass, RepairScratch* rs) {
+    const hf_patch P = R.patches[blockIdx.y];
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)P.nx * P.ny) return;
+    const int64_t c = R.base[blockIdx.y] + idx;
+    if (R.leaf && !R.leaf[c]) return;
+    const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
+    const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+        const double v = R.U[g + n * P.comp_stride];
+        if (!(v > 0.0)) continue;
+        const double m = v * R.vol;
+        if (pass == 0) {
+            atomicMax(&rs->peak_bits[n], (unsigned long long)__double_as_longlong(v));
+            if (m > 0.0) atomicMax(&rs->mass_bits[n], (unsigned long long)__double_as_longlong(m));
+        } else if (m > 0.0 && (unsigned long long)__double_as_longlong(m) == rs->mass_bits[n]) {
+            atomicMin(&rs->donor[n], repair_key(l, c));
+        }
+    }
+}
+
+template <int NS>
+__global__ void k_crep_apply(RepairLevel R, int l, RepairScratch* rs, DevStatus* st) {
+    const hf_patch P = R.patches[blockIdx.y];
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)P.nx * P.ny) return;
+    const int64_t c = R.base[blockIdx.y] + idx;
+    if (R.leaf && !R.leaf[c]) return;
+    const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
+    const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+        double& u = R.U[g + n * P.comp_stride];
+        const double v = u;
+        if (v >= 0.0) continue;
+        const double peak = __longlong_as_double((long long)rs->peak_bits[n]);
+        if (!isfinite(v) || -v > 64.0 * 2.220446049250313e-16 * peak) {
+            atomicOr(&st->flags, ST_MATERIAL);
+            atomicMin(&st->bad_cell, (unsigned long long)c);
+            continue;
+        }
+        const double d = -v * R.vol;
+        atomicAdd(&rs->deficit[n], d);
+        const unsigned long long k = atomicAdd(&rs->count, 1ull);
+        if (k < (unsigned long long)REPAIR_CAP) {
+            rs->key[k] = ((unsigned long long)n << 60) | repair_key(l, c);
+            rs->val[k] = d;
+        }
+        atomicAdd(&st->repairs, 1ull);
+        u = 0.0;
+    }
+}
+
+constexpr int REPAIR_FIX_THREADS = 1024;
+__global__ void __launch_bounds__(REPAIR_FIX_THREADS) k_crep_fix(RepairLevels R, int ns, RepairScratch* rs,
+                                                                  DevStatus* st) {
+    __shared__ unsigned long long sk[REPAIR_CAP];
+    __shared__ double sv[REPAIR_CAP];
+    __shared__ double def[16];
+    const unsigned long long cnt = rs->count;
+    if (cnt == 0) return;
+    const int t = threadIdx.x;
+    if (cnt <= (unsigned long long)REPAIR_CAP) {
+        int n2 = 2;
+        while ((unsigned long long)n2 < cnt) n2 <<= 1;
+        for (int i = t; i < n2; i += blockDim.x) {
+            const bool in = (unsigned long long)i < cnt;
+            sk[i] = in ? rs->key[i] : ~0ull;
+            sv[i] = in ? rs->val[i] : 0.0;
+        }
+        __syncthreads();
+        for (int k = 2; k <= n2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = t; i < n2; i += blockDim.x) {
+                    const int o = i ^ j;
+                    if (o > i && ((sk[i] > sk[o]) == ((i & k) == 0))) {
+                        const unsigned long long a = sk[i];
+                        sk[i] = sk[o];
+                        sk[o] = a;
+                        const double b = sv[i];
+                        sv[i] = sv[o];
+                        sv[o] = b;
+                    }
+                }
+                __syncthreads();
+            }
+        if (t < ns) {
+            double sum = 0.0;
+            for (unsigned long long i = 0; i < cnt; ++i)
+                if ((int)(sk[i] >> 60) == t) sum += sv[i];
+            def[t] = sum;
+        }
+    } else if (t < ns) {
+        def[t] = rs->deficit[t];  // more entries than the sort holds: atomic order
+    }
+    __syncthreads();
+    if (t >= ns) return;
+    const double d = def[t];
+    if (!(d > 0.0)) return;
+    const unsigned long long key = rs->donor[t];
+    const double mass = __longlong_as_double((long long)rs->mass_bits[t]);
+    if (key == ~0ull || !(mass > d)) {
+        atomicOr(&st->flags, ST_MATERIAL);
+        return;
+    }
+    const int l = (int)((key >> 52) & 0xffull);
+    const int64_t c = (int64_t)(key & ((1ull << 52) - 1));
+    const RepairLevel& L = R.lev[l];
+    for (int p = 0; p < L.npatch; ++p) {
+        const hf_patch& P = L.patches[p];
+        const int64_t b = L.base[p];
+        if (c >= b && c < b + (int64_t)P.nx * P.ny) {
+            const int64_t k = c - b;
+            const int i = (int)(k % P.nx), j = (int)(k / P.nx);
+            L.U[P.offset + (int64_t)t * P.comp_stride + (int64_t)(j + P.ng) * P.pitch + (i + P.ng)] -= d / L.vol;
+            return;
+        }
+    }
+    atomicOr(&st->flags, ST_MATERIAL);  // unreachable for keys the scan wrote
+}
+
+size_t repair_scratch_bytes() { return sizeof(RepairScratch); }
+
+cudaError_t launch_composite_repair(int ns, const RepairLevels& R, RepairScratch* rs, DevStatus* st, cudaStream_t s,
+                                    int64_t* launches) {
+    cudaError_t e = cudaMemsetAsync(rs, 0, offsetof(RepairScratch, key), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(rs->donor, 0xff, sizeof(rs->donor), s);
+    if (e != cudaSuccess) return e;
+    for (int pass = 0; pass < 3; ++pass)
+        for (int l = 0; l < R.nlev; ++l) {
+            const RepairLevel& L = R.lev[l];
+            if (L.npatch <= 0) continue;
+            const dim3 grid((unsigned)((L.max_cells + 127) / 128), (unsigned)L.npatch);
+            if (pass < 2) {
+                if (ns == 9) k_crep_scan<9><<<grid, 128, 0, s>>>(L, l, pass, rs);
+                else k_crep_scan<10><<<grid, 128, 0, s>>>(L, l, pass, rs);
+            } else {
+                if (ns == 9) k_crep_apply<9><<<grid, 128, 0, s>>>(L, l, rs, st);
+                else k_crep_apply<10><<<grid, 128, 0, s>>>(L, l, rs, st);
+            }
+            ++*launches;
+        }
+    k_crep_fix<<<1, REPAIR_FIX_THREADS, 0, s>>>(R, ns, rs, st);
+    ++*launches;
     return cudaGetLastError();
 }
 

@@ -10,11 +10,12 @@
 // affine and make regridding a change of the block list.
 //
 // Per stage (BlockAMR::euler, :202-264): ghosts of every level are filled (physical
-// boundaries and in-place neighbours by hf_fill_ghosts, coarse-fine ghosts by
-// ConservativeInterp from the next coarser level, coarse levels first), every level's
-// active blocks take the Euler update with face fluxes kept, then finest to coarsest:
-// reflux of the coarse level from the fine fluxes (FluxRegister) and average_down.
-// A stage inadmissible at second order is redone first order on all levels.
+// boundaries and in-place neighbours, coarse-fine ghosts by ConservativeInterp from the
+// next coarser level, coarse levels first), every level's active blocks take the Euler
+// update with face fluxes kept, then finest to coarsest: reflux of the coarse level from
+// the fine fluxes (FluxRegister) and average_down; then repairRoundoff over the leaf
+// cells of every level (:299-334), average_down, and validation of every level.  A
+// stage that fails the repair or the validation is redone first order on all levels.
 // flow(h) = two stages and the Heun combination (:266-270); react(dt) advances the
 // leaf cells of every level (:271-285); a failed step rolls back and halves dt.
 //
@@ -29,7 +30,9 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 #include "hf_internal.h"
 #include "mech_h2li.h"
@@ -88,6 +91,9 @@ struct hf_amr {
     // each of the two graphs is keyed by level 0's pointers; both are dropped at regrid
     hf::DevStatus* gst = nullptr;
     hf::DevStatus* gst_host = nullptr;
+    hf::DevStatus* sst = nullptr;    // per-cell checks of the flux kernels (not used: the
+                                     // composite state is checked after reflux)
+    hf::RepairScratch* rep = nullptr;
     double* ddt = nullptr;       // device [dt, dt/2]
     double* ddt_host = nullptr;
     double* key[2][4] = {};      // level 0's U, N, S, O when graph k was captured
@@ -270,37 +276,6 @@ hf_status fill_all(hf_amr* m, double* const* X, cudaStream_t s) {
     return HF_OK;
 }
 
-// One composite Euler stage in -> out (BlockAMR::euler).
-hf_status euler(hf_amr* m, double* const* in, double* const* out, double h, cudaStream_t s) {
-    hf_status r = fill_all(m, in, s);
-    if (r != HF_OK) return r;
-    for (int fo = 0; fo < 2; ++fo) {
-        r = HF_OK;
-        for (int l = 0; r == HF_OK && l <= m->finest; ++l) {
-            AmrLevel& a = m->lev[l];
-            int64_t bad = -1;
-            r = hf_flux_update(m->ctx, &a.L, a.patches.data(), (int)a.patches.size(), in[l], nullptr, out[l], a.fx, a.fy,
-                               h, fo, HF_FLUX_PLAIN, &bad, s);
-        }
-        if (r == HF_OK) {
-            if (fo) hf::ctx_add_counters(m->ctx, 1, 0);
-            break;
-        }
-        if (r != HF_ERR_INADMISSIBLE && r != HF_ERR_NEGATIVE) return r;
-    }
-    if (r != HF_OK) return r;
-    for (int l = m->finest; l > 0; --l) {
-        AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
-        r = hf_reflux(m->ctx, &c.L, c.patches.data(), (int)c.patches.size(), out[l - 1], c.fx, c.fy, f.patches.data(),
-                      (int)f.patches.size(), f.fx, f.fy, h, s);
-        if (r == HF_OK)
-            r = hf_average_down(m->ctx, f.patches.data(), (int)f.patches.size(), out[l], c.patches.data(),
-                                (int)c.patches.size(), out[l - 1], s);
-        if (r != HF_OK) return r;
-    }
-    return HF_OK;
-}
-
 hf_status average_all(hf_amr* m, double* const* X, cudaStream_t s) {
     for (int l = m->finest; l > 0; --l) {
         AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
@@ -319,6 +294,39 @@ hf_status validate_all(hf_amr* m, double* const* X, cudaStream_t s) {
         if (r != HF_OK) return r;
     }
     return HF_OK;
+}
+
+cudaError_t g_stage(hf_amr* m, double* const* in, double* const* out, double h, const double* hdev, int first_order,
+                    cudaStream_t s, int64_t* nl);
+
+// One composite Euler stage in -> out with host control (BlockAMR::euler, :202-264):
+// second order, or, when the repair or the validation of the composite state fails,
+// first order on every level (:258-263).  A face that falls back to an inadmissible
+// cell is properties() throwing inside the face loop: no redo, the step rolls back.
+hf_status euler(hf_amr* m, double* const* in, double* const* out, double h, cudaStream_t s) {
+    for (int fo = 0; fo < 2; ++fo) {
+        int64_t nl = 0;
+        cudaError_t e = cudaMemsetAsync(m->gst, 0, sizeof(hf::DevStatus), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&m->gst->bad_cell, 0xff, sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = g_stage(m, in, out, h, nullptr, fo, s, &nl);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(m->gst_host, m->gst, sizeof(hf::DevStatus), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        hf::ctx_add_launches(m->ctx, nl, 0, 0);
+        if (e != cudaSuccess) return HF_ERR_CUDA;
+        const unsigned f = m->gst_host->flags;
+        hf::ctx_add_repairs(m->ctx, (int64_t)m->gst_host->repairs);
+        if (f & hf::ST_FACE_BAD) {
+            hf::ctx_set_error(m->ctx, "amr_step: inadmissible cell state at a face");
+            return HF_ERR_FACE;
+        }
+        if (!f) {
+            if (fo) hf::ctx_add_counters(m->ctx, 1, 0);
+            return HF_OK;
+        }
+    }
+    hf::ctx_set_error(m->ctx, "amr_step: inadmissible composite state after a first-order stage");
+    return HF_ERR_INADMISSIBLE;
 }
 
 template <class F>
@@ -426,23 +434,61 @@ cudaError_t g_validate_all(hf_amr* m, double* const* X, cudaStream_t s, int64_t*
     return cudaSuccess;
 }
 
-// One composite Euler stage in -> out with h from device memory (euler()).
-cudaError_t g_euler(hf_amr* m, double* const* in, double* const* out, const double* hdev, cudaStream_t s, int64_t* nl) {
+__global__ void k_merge_face(const hf::DevStatus* from, hf::DevStatus* to) {
+    if (from->flags & hf::ST_FACE_BAD) {
+        atomicOr(&to->flags, hf::ST_FACE_BAD);
+        atomicMin(&to->bad_cell, from->bad_cell);
+    }
+}
+
+// The leaf cells of every level of X for the composite repair.
+hf::RepairLevels repair_levels(hf_amr* m, double* const* X) {
+    hf::RepairLevels R{};
+    R.nlev = m->finest + 1;
+    for (int l = 0; l <= m->finest; ++l) {
+        const AmrLevel& a = m->lev[l];
+        int64_t mc = 1;
+        for (const hf_patch& p : a.patches) mc = std::max<int64_t>(mc, (int64_t)p.nx * p.ny);
+        R.lev[l] = hf::RepairLevel{a.d_patches, a.d_base, a.leaf_mask, X[l], (int)a.patches.size(), mc,
+                                   a.L.dx * a.L.dy};
+    }
+    return R;
+}
+
+// One composite Euler stage in -> out (BlockAMR::euler, :202-264) with the stage length
+// h, or read from hdev (graph-captured steps): ghosts of every level; every level's
+// update with its face fluxes (the flux kernels' own per-cell checks go to sst and are
+// not used: the reference checks the composite state after reflux); reflux and
+// average_down from the finest level down; repairRoundoff over the leaf cells of every
+// level; average_down again (a no-op bit for bit when nothing was repaired, so it runs
+// unconditionally); validation of every level.  Face failures, material negatives and
+// inadmissible cells are flags of gst.
+cudaError_t g_stage(hf_amr* m, double* const* in, double* const* out, double h, const double* hdev, int first_order,
+                    cudaStream_t s, int64_t* nl) {
     cudaError_t e = g_fill_all(m, in, s, nl);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->sst, 0, sizeof(hf::DevStatus), s);
     for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
         AmrLevel& a = m->lev[l];
         e = hf::launch_flux_multi(m->ns, hf::make_level(a.L), a.patches.data(), a.d_patches, (int)a.patches.size(),
-                                  a.d_foff, in[l], nullptr, out[l], a.fx, a.fy, 0.0, 0, m->gst, s, nl, hdev);
+                                  a.d_foff, in[l], nullptr, out[l], a.fx, a.fy, h, first_order, m->sst, s, nl, hdev);
+    }
+    if (e == cudaSuccess) {
+        k_merge_face<<<1, 1, 0, s>>>(m->sst, m->gst);
+        ++*nl;
+        e = cudaGetLastError();
     }
     for (int l = m->finest; e == cudaSuccess && l > 0; --l) {
         AmrLevel &f = m->lev[l], &c = m->lev[l - 1];
         e = hf::launch_reflux(hf::make_level(c.L), c.d_patches, c.patches.data(), (int)c.patches.size(), c.d_xoff,
                               c.d_yoff, c.fx, c.fy, out[l - 1], f.d_patches, f.patches.data(), (int)f.patches.size(),
-                              f.d_xoff, f.d_yoff, f.fx, f.fy, c.cover, 0.0, m->nv, s, nl, hdev);
+                              f.d_xoff, f.d_yoff, f.fx, f.fy, c.cover, h, m->nv, s, nl, hdev);
         if (e == cudaSuccess)
             e = hf::launch_average_down(f.d_patches, f.patches.data(), (int)f.patches.size(), out[l], c.d_patches,
                                         (int)c.patches.size(), out[l - 1], m->nv, s, nl);
     }
+    if (e == cudaSuccess) e = hf::launch_composite_repair(m->ns, repair_levels(m, out), m->rep, m->gst, s, nl);
+    if (e == cudaSuccess) e = g_average_all(m, out, s, nl);
+    if (e == cudaSuccess) e = g_validate_all(m, out, s, nl);
     return e;
 }
 
@@ -450,8 +496,8 @@ cudaError_t g_euler(hf_amr* m, double* const* in, double* const* out, const doub
 // validation.
 cudaError_t g_flow(hf_amr* m, double* const* in, double* const* S, double* const* out, cudaStream_t s, int64_t* nl) {
     const double* half = m->ddt + 1;
-    cudaError_t e = g_euler(m, in, S, half, s, nl);
-    if (e == cudaSuccess) e = g_euler(m, S, out, half, s, nl);
+    cudaError_t e = g_stage(m, in, S, 0.0, half, 0, s, nl);
+    if (e == cudaSuccess) e = g_stage(m, S, out, 0.0, half, 0, s, nl);
     for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
         const int64_t n = (int64_t)(m->lev[l].bytes / sizeof(double));
         k_lincomb_all<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 0.5, in[l], 0.5, out[l]);
@@ -670,19 +716,34 @@ extern "C" {
 hf_status hf_amr_regrid(hf_amr* m, void* stream) {
     if (!m) return HF_ERR_ARG;
     const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // regridChecked (:367-373): average_down, totals, remap, average_down, validate,
+    // totals; the totals must survive the remap (relative to the total of the
+    // magnitudes, so that a component summing to ~0 is judged fairly)
+    double* U[8];
+    arrays(m, [](AmrLevel& a) { return a.U; }, U);
     double before[16], after[16], scale[16];
-    hf_status r = totals(m, before, s);
+    hf_status r = average_all(m, U, s);
+    if (r == HF_OK) r = totals(m, before, s);
     if (r == HF_OK) r = totals(m, scale, s, 1);
     for (int l = 0; r == HF_OK && l < m->o.max_level && l <= m->finest; ++l) r = regrid_level(m, l, s);
+    if (r == HF_OK) r = average_all(m, U, s);
+    if (r == HF_OK) {
+        r = validate_all(m, U, s);
+        if (r == HF_ERR_INADMISSIBLE) hf::ctx_set_error(m->ctx, "regrid: inadmissible cell after the remap");
+    }
     if (r == HF_OK) r = totals(m, after, s);
     if (r != HF_OK) return r;
     ++m->regrids;
     // building the hierarchy from given level states is InitFromScratch, not a remap
     if (!m->init.empty()) return HF_OK;
-    // regridChecked (:369-371): the conserved totals must survive the remap (relative to
-    // the total of the magnitudes, so that a component summing to ~0 is judged fairly)
-    for (int n = 0; n < m->nv; ++n)
-        if (std::fabs(after[n] - before[n]) > 1e-8 * scale[n]) return HF_ERR_INADMISSIBLE;
+    double defect = 0.0;
+    for (int n = 0; n < m->nv; ++n) defect = std::max(defect, std::fabs(after[n] - before[n]) / std::max(scale[n], 1e-300));
+    if (defect > 1e-8) {
+        char msg[96];
+        snprintf(msg, sizeof msg, "regrid: nonconservative remap (relative defect %.3e)", defect);
+        hf::ctx_set_error(m->ctx, msg);
+        return HF_ERR_INADMISSIBLE;
+    }
     return HF_OK;
 }
 
@@ -752,7 +813,10 @@ hf_status hf_amr_create_levels(hf_ctx* ctx, const hf_level* base, const double* 
          cudaMemset(m->gst, 0, sizeof(hf::DevStatus)) == cudaSuccess &&
          cudaMallocHost(&m->gst_host, sizeof(hf::DevStatus)) == cudaSuccess &&
          cudaMalloc(&m->ddt, 2 * sizeof(double)) == cudaSuccess &&
-         cudaMallocHost(&m->ddt_host, 2 * sizeof(double)) == cudaSuccess;
+         cudaMallocHost(&m->ddt_host, 2 * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&m->sst, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMemset(m->sst, 0, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMalloc(&m->rep, hf::repair_scratch_bytes()) == cudaSuccess;
     if (ok) {
         AmrLevel& a = m->lev[0];
         const int64_t nc = (int64_t)a.L.nx * a.L.ny;
@@ -806,6 +870,8 @@ void hf_amr_destroy(hf_amr* m) {
         if (g) cudaGraphExecDestroy(g);
     cudaFree(m->gst);
     cudaFreeHost(m->gst_host);
+    cudaFree(m->sst);
+    cudaFree(m->rep);
     cudaFree(m->ddt);
     cudaFreeHost(m->ddt_host);
     delete m;
@@ -883,6 +949,8 @@ hf_status hf_amr_step(hf_amr* m, double cfl, double* dt, void* stream) {
                 return HF_ERR_CUDA;
         h *= 0.5;  // rollback (:413-418)
     }
+    std::string msg = std::string("amr_step: time advancement failed; last attempt: ") + hf_last_error(m->ctx);
+    hf::ctx_set_error(m->ctx, msg.c_str());
     return HF_ERR_INADMISSIBLE;
 }
 

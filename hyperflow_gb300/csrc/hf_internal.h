@@ -53,6 +53,9 @@ inline Level make_level(const hf_level& l) {
 
 // Counter updates from the host stepper (hf_abi.cu)
 void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries);
+void ctx_add_repairs(hf_ctx* ctx, int64_t repairs);
+// The message hf_last_error returns, for failures found outside hf_abi.cu
+void ctx_set_error(hf_ctx* ctx, const char* msg);
 // Counters and device time of work run outside the ABI entry points (graph-captured steps)
 void ctx_add_launches(hf_ctx* ctx, int64_t kernels, int64_t chem_cells, int64_t chem_steps);
 bool ctx_timing_enabled(const hf_ctx* ctx);
@@ -178,5 +181,39 @@ cudaError_t launch_reflux(const Level& L, const hf_patch* coarse_dev, const hf_p
                           const double* hdev = nullptr);
 cudaError_t launch_chem_commit(int ns, double* U, int64_t comp_stride, const int64_t* cell_index,
                                int64_t count, const double* trial, cudaStream_t s, int64_t* launches);
+
+// Composite roundoff repair (hf_amr.cu): repairRoundoff over the leaf cells of several
+// levels.  Each level gives its patch table and first-cell offsets (device), an
+// optional leaf mask over its patch-packed cells (null: every cell is a leaf), its
+// state and its cell volume; npatch and max_cells (the largest patch's cell count) are
+// host values for the launch shape.
+constexpr int REPAIR_CAP = 2048;  // negative entries summed in the reference's order
+constexpr int REPAIR_MAX_LEVELS = 8;
+struct RepairLevel {
+    const hf_patch* patches;
+    const int64_t* base;
+    const uint8_t* leaf;
+    double* U;
+    int npatch;
+    int64_t max_cells;
+    double vol;
+};
+struct RepairLevels {
+    RepairLevel lev[REPAIR_MAX_LEVELS];
+    int nlev;
+};
+struct RepairScratch {  // device memory, cleared by every launch_composite_repair
+    unsigned long long peak_bits[16];
+    unsigned long long mass_bits[16];
+    double deficit[16];          // atomic deficit sums (used past REPAIR_CAP entries)
+    unsigned long long count;    // negative entries found
+    unsigned long long donor[16];
+    unsigned long long key[REPAIR_CAP];  // species << 60 | level << 52 | cell
+    double val[REPAIR_CAP];              // deficit of the entry (-value x volume)
+};
+size_t repair_scratch_bytes();
+// Flags ST_MATERIAL in st and adds the number of zeroed values to st->repairs.
+cudaError_t launch_composite_repair(int ns, const RepairLevels& R, RepairScratch* rs, DevStatus* st, cudaStream_t s,
+                                    int64_t* launches);
 
 }  // namespace hf

@@ -613,6 +613,38 @@ def totals(ctx, pset, cell_volume, leaf_mask=None, absolute=False):
     return [out[n] for n in range(pset.nv)]
 
 
+def repair_roundoff(ctx, parts):
+    """BlockAMR::repairRoundoff (BlockAMR.cpp:299-334) in place over the leaf cells of one
+    or more levels.  parts: [(level, PatchSet or PatchArray, leaf mask or None), ...],
+    coarsest level first; a leaf mask is a uint8 CUDA tensor over the patches' cells packed
+    in order, row-major (None: every cell is a leaf).  Returns the number of values set to
+    zero; raises DomainError (HF_ERR_NEGATIVE) when a value is materially negative or a
+    donor holds too little mass."""
+    n = len(parts)
+    levels = (L.Level * n)()
+    pp = (ctypes.POINTER(L.Patch) * n)()
+    npatch = (ctypes.c_int * n)()
+    U = (ctypes.c_void_p * n)()
+    leaf = (ctypes.c_void_p * n)()
+    keep = []
+    for k, (lv, ps, mask) in enumerate(parts):
+        levels[k] = lv
+        if isinstance(ps, PatchArray):
+            arr = (L.Patch * 1)(ps.patch)
+            keep.append(arr)
+            pp[k] = ctypes.cast(arr, ctypes.POINTER(L.Patch))
+            npatch[k] = 1
+        else:
+            pp[k] = ctypes.cast(ps.patches, ctypes.POINTER(L.Patch))
+            npatch[k] = len(ps)
+        U[k] = _ptr(ps.data)
+        leaf[k] = _ptr(mask)
+    rep = ctypes.c_int64(0)
+    ctx.check(ctx.lib.hf_repair_roundoff(ctx.h, n, levels, pp, npatch, U, leaf, ctypes.byref(rep), _stream()),
+              "repair_roundoff")
+    return rep.value
+
+
 def average_down(ctx, fine, coarse):
     """Every coarse cell under a fine patch becomes the mean of its four children."""
     ctx.check(ctx.lib.hf_average_down(ctx.h, fine.patches, len(fine), _ptr(fine.data), coarse.patches, len(coarse),

@@ -112,7 +112,9 @@ HF_EXPORT void hf_get_counters(const hf_ctx* ctx, hf_counters* out);
 HF_EXPORT void hf_set_timing(hf_ctx* ctx, int enable);
 HF_EXPORT void hf_get_timing(const hf_ctx* ctx, double ms[3], int64_t launches[3]);
 /* Multiply each reaction's pre-exponential factor(s) by scale[r] (21 entries; NULL resets).
- * Used for d/d ln A_k sensitivity checks; not in the reference. */
+ * Used for d/d ln A_k sensitivity checks; not in the reference.  The factors live in
+ * constant memory, one copy per device and process: the scale applies to every context
+ * on the current device and to hf_chem_advance_noalloc until it is reset. */
 HF_EXPORT hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale);
 
 /* Measured FP64 FMA throughput of the device (GFLOP/s, FMA = 2 flops): the FP64 roofline
@@ -271,18 +273,21 @@ HF_EXPORT hf_status hf_flux_adjoint(hf_ctx* ctx, const hf_level* level, const hf
 
 /* Chemistry without any device allocation.  No counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc: code running while a stream is being captured
- * into a CUDA graph, host code that must not synchronise the device through the allocator,
- * or an embedding application whose memory budget is fixed up front and reserved for its
- * own pool.  It needs no hf_ctx (hf_init allocates).  It runs the plain form of
- * hf_chem_advance (one thread per cell, same results, same all-or-nothing semantics and
- * error codes) with its scratch (trial states, failure codes, status word) in one
- * statically sized device array that every GPU loading this library holds until the
- * process exits: HF_NOALLOC_MAX_CELLS cells, about 1.8 MB.
+ * For callers that cannot call cudaMalloc: an embedding application whose device memory
+ * budget is fixed up front and handed to its own pool (so a library allocation fails or
+ * breaks the budget), or host code that must not take the device-wide synchronisation
+ * that cudaMalloc and cudaFree can imply.  It needs no hf_ctx (hf_init allocates).  It
+ * runs the plain form of hf_chem_advance (one thread per cell, same results, same
+ * all-or-nothing semantics and error codes) with its scratch (trial states, failure
+ * codes, status word) in one statically sized device array that every GPU loading this
+ * library holds until the process exits: HF_NOALLOC_MAX_CELLS cells, about 1.8 MB.
  *   - nspecies: 9 (H2_Li) or 10 (H2_Li+AR); count > HF_NOALLOC_MAX_CELLS -> HF_ERR_ARG.
+ *   - The call reads its status word back to the host and synchronises the stream before
+ *     it commits the batch (all-or-nothing).
  *   - The first call on a device (the current device) looks up the array's device address
- *     and, if no hf_ctx has done so on that device, loads the rate constants; make that
- *     first call before any stream capture.
+ *     and, if no hf_ctx has loaded the rate constants on that device, loads them.
+ *   - The rate constants are the device's current ones: hf_set_rate_scale on any context
+ *     in the process rescales them for this call too (they are one per device).
  *   - Every call uses the same array: calls that overlap on the GPU (other streams or
  *     threads) race.  Each call clears the status word it needs before launching.
  * Arguments as hf_chem_advance without ctx and form. */
@@ -405,6 +410,21 @@ HF_EXPORT hf_status hf_cfl_dt(hf_ctx* ctx, const hf_level* level, const hf_patch
  * linear cell index if any valid cell is inadmissible. */
 HF_EXPORT hf_status hf_validate(hf_ctx* ctx, const hf_level* level, const hf_patch* patches, int npatch,
                       const double* U, int64_t* bad_cell, void* stream);
+/* BlockAMR::repairRoundoff (BlockAMR.cpp:299-334) over the leaf cells of nlev levels, in
+ * place: per species the peak partial density and the donor (the first cell, levels in
+ * order, patches in order, cells row by row, holding the largest mass = value x cell
+ * volume) over all leaf cells; a value below zero by at most 64 ulp of the peak is set
+ * to zero and its deficit (-value x volume) taken from the donor, the deficits added in
+ * that cell order.  HF_ERR_NEGATIVE if a value is further below zero or not finite, or a
+ * donor holds no more mass than its deficit (the reference throws); the state may then
+ * be partly repaired.  Level l: levels[l] (its dx, dy give the cell volume),
+ * patches[l][0..npatch[l]-1], state U[l], and leaf[l] (nullable: every cell is a leaf), a
+ * device byte mask over the patches' cells packed in order, row-major.  *repairs (may be
+ * NULL): the number of values set to zero.  The stepper calls the same kernels after
+ * every stage (one level: hf_flux_update; every level after reflux: hf_amr_step). */
+HF_EXPORT hf_status hf_repair_roundoff(hf_ctx* ctx, int nlev, const hf_level* levels, const hf_patch* const* patches,
+                                       const int* npatch, double* const* U, const uint8_t* const* leaf,
+                                       int64_t* repairs, void* stream);
 
 /* ---- host stepper over a single-patch uniform level (BlockAMR::run loop body,
  * BlockAMR.cpp:409-419): Strang flow(dt/2), react(dt), flow(dt/2), each flow a Heun pair

@@ -15,9 +15,11 @@ on levels 0..max_level of a domain with the reference's boundary conditions.
 - Euler stage: level 0 as one box, level l >= 1 block by block (a block face is a wall
   face only where it lies on a reflecting or wedge domain edge), then from the finest
   level down: reflux of level l-1 from level l's face fluxes (FluxRegister, :245-256)
-  and average_down (:256).  A stage whose updated cells are inadmissible on any level
-  is redone first order on every level (:258-263); species below zero by at most 64
-  ulp of their peak are repaired first, level by level (repairRoundoff, :299-334).
+  and average_down (:256), then repairRoundoff over the leaf cells of every level
+  (:299-334: species below zero by at most 64 ulp of their peak zeroed, the deficit
+  taken from the cell holding the most mass), average_down again if a value was
+  repaired, and validation of every level; a stage that fails the repair or the
+  validation is redone first order on every level (:258-263).
 - flow(h): two stages, Heun combination, average_down, validation.
 - step(dt): flow(dt/2), react(dt), flow(dt/2); a failed attempt is rolled back and
   retried with half the step (:411-419).
@@ -29,8 +31,9 @@ on levels 0..max_level of a domain with the reference's boundary conditions.
   footprint grown by tag_buffer cells and the footprint grown by 2 cells lies in active
   level-l cells (proper nesting); both wrap across periodic edges and are cut at the
   others.  Blocks that become active are filled by ConservativeInterp from level l;
-  blocks that stay keep their data; nothing is averaged.  The leaf totals must survive
-  the remap to 1e-8 of the total of the magnitudes (regridChecked, :369-371).  The block
+  blocks that stay keep their data.  As regridChecked (:367-373) the hierarchy is
+  averaged down before and after the remap and validated after it, and the leaf totals
+  must survive the remap to 1e-8 of the total of the magnitudes.  The block
   rule is the GPU stepper's deterministic choice in place of AMReX's clustering.
 States are AoS arrays (..., NS+3); levels are dense ghosted arrays (ny+4, nx+4, NV).
 """
@@ -235,7 +238,8 @@ class Hierarchy:
 
     def _stages(self, Xin, h, first_order):
         """Every level's Euler update from the filled Xin: (out, whole-level face fluxes,
-        per-block fine fluxes, admissible)."""
+        per-block fine fluxes).  No cell check here: the reference checks the composite
+        state after reflux and average_down."""
         out = [x.copy() for x in Xin]
         B = self.B
         FX, FY, fine = [], [], []
@@ -267,69 +271,95 @@ class Hierarchy:
             FX.append(fxa)
             FY.append(fya)
             fine.append((boxes, fxl, fyl))
-        ok = all(self._stage_ok(out, l) for l in range(self.finest + 1))
-        return out, FX, FY, fine, ok
+        return out, FX, FY, fine
 
-    def _stage_ok(self, X, l):
-        """The per-level check after an update (repairRoundoff and validate,
-        BlockAMR.cpp:286-334, over the level's active cells in block order): a species
-        below zero by at most 64 ulp of its peak is zeroed and its mass taken from the
-        first cell holding the peak; a larger or non-finite negative value, or a donor
-        too small, fails the stage, and so does an inadmissible cell.  X[l] is repaired
-        in place."""
-        B, ns = self.B, self.nv - 3
-        if l == 0:
-            views = [X[0][2:-2, 2:-2]]
-        else:
-            views = [X[l][2 + bj * B:2 + (bj + 1) * B, 2 + bi * B:2 + (bi + 1) * B] for bi, bj in self.blocks(l)]
-        cells = np.concatenate([v.reshape(-1, self.nv) for v in views])
-        sp = cells[:, :ns]
-        if np.any(sp < 0) or np.any(~np.isfinite(sp)):
-            dx, dy = self.dxs[l]
-            vol = dx * dy
-            peak = np.where(sp > 0, sp, 0.0).max(0)
-            bad = ~np.isfinite(sp) | ((sp < 0) & (-sp > 64 * np.finfo(np.float64).eps * peak))
-            if bad.any():
-                return False
-            deficit, count = np.zeros(ns), 0
-            for n in range(ns):
-                neg = np.nonzero(sp[:, n] < 0)[0]
-                if not len(neg):
-                    continue
-                for k in neg:
-                    deficit[n] += -sp[k, n] * vol
-                    sp[k, n] = 0.0
-                count += len(neg)
-                if not peak[n] * vol > deficit[n]:
-                    return False
-                donor = int(np.nonzero(sp[:, n] == peak[n])[0][0])
-                sp[donor, n] -= deficit[n] / vol
-            cells[:, :ns] = sp
-            k = 0
-            for v in views:
-                n = v.shape[0] * v.shape[1]
-                v[:] = cells[k:k + n].reshape(v.shape)
-                k += n
-            self.roundoff_repairs += count
-        return not np.any(oracle.properties(cells)[3])
+    def _patches(self, l):
+        """The GPU stepper's patches of level l in table order, as (j0, i0, ny, nx): the
+        whole level when every block is active (level 0 always), else the active blocks
+        in row-major block order."""
+        ny, nx = self.shape[l]
+        if l == 0 or self.acts[l].all():
+            return [(0, 0, ny, nx)]
+        B = self.B
+        return [(bj * B, bi * B, B, B) for bi, bj in self.blocks(l)]
+
+    def repair(self, X):
+        """repairRoundoff (BlockAMR.cpp:299-334) over the leaf cells of every level, cells
+        taken in the order levels, patches (`_patches`), rows: per species the peak partial
+        density and the donor (the first cell holding the largest mass, value x volume)
+        over all leaf cells; a value below zero by more than 64 ulp of the peak, or not
+        finite, is material; smaller ones are zeroed and their deficits (-value x volume)
+        added in cell order and taken from the donor, which must hold more mass than the
+        deficit.  X is repaired in place.  Returns (ok, number of zeroed values)."""
+        ns, eps = self.nv - 3, np.finfo(np.float64).eps
+        locs, vols = [], []
+        for l in range(self.finest + 1):
+            leaf = self.leaf_mask(l)
+            vol = self.dxs[l][0] * self.dxs[l][1]
+            for j0, i0, pny, pnx in self._patches(l):
+                jj, ii = np.mgrid[j0:j0 + pny, i0:i0 + pnx]
+                jj, ii = jj.reshape(-1), ii.reshape(-1)
+                keep = leaf[jj, ii]
+                locs.append((l, jj[keep], ii[keep]))
+                vols.append(np.full(int(keep.sum()), vol))
+        v = np.concatenate([X[l][jj + 2, ii + 2, :ns] for l, jj, ii in locs])
+        vol = np.concatenate(vols)
+        neg = ~(v >= 0)
+        if not neg.any():
+            return True, 0
+        peak = np.where(v > 0, v, 0.0).max(0)
+        mass = np.where(v > 0, v * vol[:, None], 0.0)
+        if np.any(neg & (~np.isfinite(v) | (-v > 64 * eps * peak))):
+            return False, 0
+        count = 0
+        for n in range(ns):
+            k = np.nonzero(neg[:, n])[0]
+            if not len(k):
+                continue
+            d = 0.0
+            for kk in k:
+                d += float(-v[kk, n] * vol[kk])
+            v[k, n] = 0.0
+            count += len(k)
+            if not d > 0:
+                continue
+            donor = int(np.argmax(mass[:, n]))
+            if not mass[donor, n] > d:
+                return False, count
+            v[donor, n] -= d / vol[donor]
+        k = 0
+        for l, jj, ii in locs:
+            X[l][jj + 2, ii + 2, :ns] = v[k:k + len(jj)]
+            k += len(jj)
+        self.roundoff_repairs += count
+        return True, count
+
+    def _valid(self, X):
+        return not any(np.any(oracle.properties(self._active_cells(X, l))[3]) for l in range(self.finest + 1))
 
     def euler(self, Xin, h):
-        """One composite stage: second order, or first order on every level when a level's
-        updated cells are inadmissible (BlockAMR.cpp:258-263)."""
+        """One composite stage (BlockAMR::euler, :202-264): every level's update, then from
+        the finest level down reflux and average_down, then repairRoundoff over the leaf
+        cells of every level, average_down again when a value was repaired, and validation
+        of every level; when the repair or the validation fails the whole stage is redone
+        first order (:258-263), and a failing first-order stage fails the step."""
         Xin = self.fill([x.copy() for x in Xin])
-        out, FX, FY, fine, ok = self._stages(Xin, h, False)
-        if not ok:
-            out, FX, FY, fine, ok = self._stages(Xin, h, True)
-            if not ok:
-                raise StepFailure("inadmissible cell after a first-order stage")
-            self.first_order_stages += 1
-        for l in range(self.finest, 0, -1):
-            boxes, fxl, fyl = fine[l]
-            dx, dy = self.dxs[l - 1]
-            out[l - 1][2:-2, 2:-2] = oracle.reflux(out[l - 1][2:-2, 2:-2], FX[l - 1], FY[l - 1], boxes, fxl, fyl, h, dx,
-                                                   dy, periodic=(self.px, self.py))
-            out[l - 1] = self._averaged(l, out[l], out[l - 1])
-        return out
+        for first_order in (False, True):
+            out, FX, FY, fine = self._stages(Xin, h, first_order)
+            for l in range(self.finest, 0, -1):
+                boxes, fxl, fyl = fine[l]
+                dx, dy = self.dxs[l - 1]
+                out[l - 1][2:-2, 2:-2] = oracle.reflux(out[l - 1][2:-2, 2:-2], FX[l - 1], FY[l - 1], boxes, fxl, fyl, h,
+                                                       dx, dy, periodic=(self.px, self.py))
+                out[l - 1] = self._averaged(l, out[l], out[l - 1])
+            ok, repaired = self.repair(out)
+            if ok and repaired:
+                out = self.average_all(out)
+            if ok and self._valid(out):
+                if first_order:
+                    self.first_order_stages += 1
+                return out
+        raise StepFailure("inadmissible cell after a first-order stage")
 
     def flow(self, h):
         U = self.X
@@ -440,16 +470,24 @@ class Hierarchy:
         self._rebuild()
 
     def regrid(self):
+        """regridChecked (BlockAMR.cpp:367-373): average_down, the totals, the remap level by
+        level, average_down, validation, and the totals again, which must agree to 1e-8 of
+        the total of the magnitudes (not checked while the hierarchy is built from given
+        level states)."""
+        self.X = self.average_all(self.X)
         before, scale = self.totals(), self.totals(absolute=True)
         l = 0
         while l < self.max_level and l <= self.finest:
             self._regrid_level(l)
             l += 1
+        self.X = self.average_all(self.X)
+        if not self._valid(self.X):
+            raise RuntimeError("regridChecked: inadmissible cell after the remap")
         self.regrids += 1
         if self._init:
             return  # building the hierarchy from given level states is not a remap
         after = self.totals()
-        if np.any(np.abs(after - before) > 1e-8 * scale):
+        if np.any(np.abs(after - before) > 1e-8 * np.maximum(scale, 1e-300)):
             raise RuntimeError("regridChecked: the totals changed in the remap")
 
     # ------------------------------------------------------------ results

@@ -319,6 +319,15 @@ def euler_stage(g, Ug, h, first_order=False):
     return out, fx, fy, st
 
 
+def repair_roundoff(g, U):
+    """repairRoundoff (BlockAMR.cpp:299-334) of a one-level ghosted state (every cell a
+    leaf): (repaired copy, status 0 ok / 1 material or insufficient donor, zeroed count)."""
+    U = np.ascontiguousarray(U, dtype=np.float64).copy()
+    n = ctypes.c_long(0)
+    st = lib().or_repair_roundoff(ctypes.byref(g), _p(U), ctypes.byref(n))
+    return U, st, n.value
+
+
 def flow(g, U, h):
     U = np.ascontiguousarray(U, dtype=np.float64).copy()
     s = Stats()

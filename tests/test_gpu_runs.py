@@ -263,7 +263,9 @@ def test_run_amr_case_writes_reference_files(gpu, tmp_path):
     names = sorted(os.listdir(tmp_path))
     assert names == ["boxes_0.csv", "boxes_1.csv", "boxes_2.csv", "history.csv", "state_0.csv", "state_1.csv",
                      "state_2.csv", "summary.json"]
+    # the composite oracle takes 5 steps here without a retry (tests/test_output_amr.py)
     assert s["completed"] and s["final_time"] == 2e-8 and s["retries"] == 0 and s["finest_level"] >= 1
+    assert s["steps"] == 5
     for k in range(3):
         data = np.genfromtxt(tmp_path / ("state_%d.csv" % k), names=True, delimiter=",")
         check_geometry(data, (32, 16), (32 * lvd["dx"], 16 * lvd["dy"]), int(data["level"].max()))

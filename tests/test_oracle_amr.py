@@ -225,10 +225,12 @@ def test_walled_partial_refinement_conserves(oracle, amr_oracle):
     assert abs(t1[ns + 2] - t0[ns + 2]) <= 1e-12 * abs(t0[ns + 2])
 
 
-def test_stage_check_repairs_roundoff_negatives(oracle, amr_oracle):
-    """repairRoundoff on a block level: a species a few ulp below zero is zeroed and its
-    mass taken from the first cell holding the level's peak; one far below zero fails
-    the stage (BlockAMR.cpp:299-334)."""
+def test_composite_repair_of_roundoff_negatives(oracle, amr_oracle):
+    """repairRoundoff over the leaf cells of both levels (BlockAMR.cpp:299-334): a species a
+    few ulp below zero on a level-1 block and on an uncovered level-0 cell is zeroed, the
+    deficit taken from the leaf cell holding the most mass of it (value x volume, over
+    both levels), so the leaf total is kept; a negative under a fine block is not a leaf
+    and stays; one far below zero fails."""
     nx, ny, B, dx = 32, 16, 8, 1e-4
     U0 = H.smooth_field(nx, ny, seed=5)
     U1 = H.smooth_field(2 * nx, 2 * ny, seed=6)
@@ -236,18 +238,26 @@ def test_stage_check_repairs_roundoff_negatives(oracle, amr_oracle):
     active[:, 2:5] = 1
     a = amr_oracle.AmrOracle(U0, U1, active, dx, dx, B)
     X = [x.copy() for x in a.X]
-    lv = X[1][2:-2, 2:-2]
-    cells = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12) for bi, bj in a.blocks(1)])
-    peak = cells[:, 5].max()
-    lv[3, 20, 5] = -2e-16 * peak      # within 64 ulp: repaired
-    total = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12)
-                            for bi, bj in a.blocks(1)])[:, 5].sum()
-    assert a._stage_ok(X, 1)
-    assert lv[3, 20, 5] == 0.0 and a.roundoff_repairs == 1
-    cells = np.concatenate([lv[bj * B:(bj + 1) * B, bi * B:(bi + 1) * B].reshape(-1, 12) for bi, bj in a.blocks(1)])
-    assert abs(cells[:, 5].sum() - total) <= 1e-14 * total
-    lv[5, 22, 5] = -1e-3 * peak       # materially negative: the stage fails
-    assert not a._stage_ok(X, 1)
+    l0, l1 = X[0][2:-2, 2:-2], X[1][2:-2, 2:-2]
+    m0, m1 = a.leaf_mask(0), a.leaf_mask(1)
+    vol = [dx * dx, dx * dx / 4]
+
+    def leaf_total(n):
+        return (l0[m0][:, n].sum() * vol[0]) + (l1[m1][:, n].sum() * vol[1])
+
+    peak = max(l0[m0][:, 5].max(), l1[m1][:, 5].max())
+    l1[3, 20, 5] = -2e-16 * peak      # leaf on level 1, within 64 ulp
+    l0[2, 1, 5] = -1e-16 * peak       # leaf on level 0
+    l0[4, 10, 5] = -1e-3 * peak       # covered by the level-1 block over columns 8..19: not a leaf
+    assert m1[3, 20] and m0[2, 1] and not m0[4, 10]
+    total = leaf_total(5)
+    ok, count = a.repair(X)
+    assert ok and count == 2 and a.roundoff_repairs == 2
+    assert l1[3, 20, 5] == 0.0 and l0[2, 1, 5] == 0.0 and l0[4, 10, 5] < 0
+    assert abs(leaf_total(5) - total) <= 1e-14 * abs(total)
+    l1[5, 22, 5] = -1e-3 * peak       # materially negative leaf value
+    ok, _ = a.repair(X)
+    assert not ok
 
 
 def test_rollback_halves_like_the_one_level_run(oracle, amr_oracle):

@@ -138,8 +138,15 @@ class OracleAmr:
 
 
 class CountingCtx:
+    """The counters run_amr_case reads, taken from the composite oracle behind the stepper."""
+
+    def __init__(self, stepper):
+        self.h = stepper.h
+
     def counters(self):
-        return {"retries": 0, "first_order_stages": 0, "roundoff_repairs": 0, "chem_cell_calls": 0}
+        h = self.h
+        return {"retries": h.retries, "first_order_stages": h.first_order_stages,
+                "roundoff_repairs": h.roundoff_repairs, "chem_cell_calls": 0}
 
 
 def test_run_amr_case_host_logic(oracle, out, tmp_path):
@@ -165,7 +172,7 @@ def test_run_amr_case_host_logic(oracle, out, tmp_path):
         return p, T
 
     end = 5.5 * dt
-    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0.transpose(2, 0, 1).copy()), end,
+    s = out.run_amr_case(CountingCtx(stepper), S.make_level(**lvd), torch.from_numpy(U0.transpose(2, 0, 1).copy()), end,
                          str(tmp_path), cfl=0.5, output_times=[2.5 * dt, end], max_level=2, block=B, tag_buffer=1,
                          regrid_interval=2, chemistry=False, stepper=stepper, props=props)
     import os
@@ -209,7 +216,7 @@ def test_reference_blast_config_through_the_amr_runner(oracle, out, tmp_path):
         assert not np.any(st)
         return p, T
 
-    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+    s = out.run_amr_case(CountingCtx(stepper), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
                          cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
                          block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
                          chemistry=True, stepper=stepper, props=props)
@@ -245,7 +252,7 @@ def test_reference_inert_blast_config_through_the_amr_runner(oracle, out, tmp_pa
         assert not np.any(st)
         return p, T
 
-    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+    s = out.run_amr_case(CountingCtx(stepper), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
                          cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
                          block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
                          chemistry=False, stepper=stepper, props=props)
@@ -285,7 +292,7 @@ def test_reference_moving_refinement_config_through_the_amr_runner(oracle, out, 
         assert not np.any(st)
         return p, T
 
-    s = out.run_amr_case(CountingCtx(), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
+    s = out.run_amr_case(CountingCtx(stepper), S.make_level(**lvd), torch.from_numpy(U0), run["end_time"], str(tmp_path),
                          cfl=run["cfl"], output_times=run["output_times"], max_level=run["max_level"],
                          block=run["block"], tag_buffer=run["tag_buffer"], regrid_interval=run["regrid_interval"],
                          chemistry=False, stepper=stepper, props=props)
@@ -293,5 +300,35 @@ def test_reference_moving_refinement_config_through_the_amr_runner(oracle, out, 
     last = stepper.h.acts[2]
     assert np.any(last & (1 - first)) and np.any(first & (1 - last))
     summ = json.loads((tmp_path / "summary.json").read_text())
+    a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
+    assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
+
+
+def test_reacting_detonation_through_the_amr_runner_takes_no_retry(oracle, out, tmp_path):
+    """The three-level reacting detonation of the GPU runner test (32 x 16 periodic, N2
+    diluent, blocks of 16, regrid every 2 steps) over the composite oracle: with the
+    roundoff repair after reflux over every level's leaf cells (BlockAMR.cpp:257), no step
+    is rolled back.  A repair level by level before the reflux leaves a coarse trace
+    species a few ulp below zero next to a fine block, which fails validation at any step
+    size until the step is small enough to change nothing."""
+    import amr
+    import torch
+    from hyperflow_gb300 import solver as S, workloads as W
+    U, lvd = W.det2d(seed=6, diluent="N2", nx=32, ny=16, hot_columns=6)
+    lvd = dict(lvd, periodic=(1, 1))
+    tags = dict(pressure_tag=0.08, temperature_tag=0.08, density_tag=0.05)
+    stepper = OracleAmr(oracle, amr, U.transpose(1, 2, 0), lvd, 16, amr.criteria(chemistry=True, **tags), 2, 1,
+                        chemistry=True)
+
+    def props(q):
+        p, _, T, st = oracle.properties(np.ascontiguousarray(q.T))
+        assert not np.any(st)
+        return p, T
+
+    s = out.run_amr_case(CountingCtx(stepper), S.make_level(**lvd), torch.from_numpy(U), 2e-8, str(tmp_path), cfl=0.5,
+                         output_times=[1e-8, 2e-8], max_level=2, block=16, tag_buffer=1, regrid_interval=2,
+                         chemistry=True, stepper=stepper, props=props)
+    assert s["completed"] and s["retries"] == 0 and s["finest_level"] == 2 and s["steps"] == 5
+    summ = __import__("json").loads((tmp_path / "summary.json").read_text())
     a, b = np.array(summ["initial_conserved_integrals"]), np.array(summ["final_conserved_integrals"])
     assert abs(b[:9].sum() / a[:9].sum() - 1) < 1e-11 and abs(b[11] / a[11] - 1) < 1e-11
