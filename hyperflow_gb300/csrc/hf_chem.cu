@@ -40,10 +40,13 @@ __device__ __forceinline__ void report(DevStatus* st, int* fail, int64_t i, int 
 template <int NS>
 __global__ void __launch_bounds__(64) k_chem_plain(const double* __restrict__ U, int64_t cs,
                                                    const int64_t* __restrict__ cell_index, int64_t count, double dt,
+                                                   const double* __restrict__ dt_dev,
                                                    const double* __restrict__ dt_cell, double rtol, double atol,
                                                    double* __restrict__ trial, int* __restrict__ fail, DevStatus* st) {
+    if (st->abort_run) return;  // an earlier step of this device-resident run failed
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
+    if (dt_dev) dt = *dt_dev;  // interval from device memory (graph-captured steps)
     double u[NS + 3];
     load_cell<NS>(U, cs, cell_index ? cell_index[i] : i, u);
     ChemCell<NS> c;
@@ -302,11 +305,11 @@ cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* id
 template <int NS>
 static cudaError_t chem_impl(int form, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
                              const double* dtc, double rtol, double atol, double* trial, int* fail, DevStatus* st,
-                             int sm_count, cudaStream_t s, int64_t* launches) {
+                             int sm_count, cudaStream_t s, int64_t* launches, const double* dt_dev) {
     const int bs = 64;
     if (form == HF_CHEM_PLAIN) {
-        k_chem_plain<NS><<<(unsigned)((count + bs - 1) / bs), bs, 0, s>>>(U, cs, idx, count, dt, dtc, rtol, atol, trial,
-                                                                          fail, st);
+        k_chem_plain<NS><<<(unsigned)((count + bs - 1) / bs), bs, 0, s>>>(U, cs, idx, count, dt, dt_dev, dtc, rtol, atol,
+                                                                          trial, fail, st);
     } else {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chem_persistent<NS>, bs, 0);
@@ -322,9 +325,11 @@ static cudaError_t chem_impl(int form, double* U, int64_t cs, const int64_t* idx
 }
 cudaError_t launch_chem(int ns, int form, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
                         const double* dtc, double rtol, double atol, double* trial, int* fail, DevStatus* st,
-                        int sm_count, cudaStream_t s, int64_t* launches) {
-    return ns == 9 ? chem_impl<9>(form, U, cs, idx, count, dt, dtc, rtol, atol, trial, fail, st, sm_count, s, launches)
-                   : chem_impl<10>(form, U, cs, idx, count, dt, dtc, rtol, atol, trial, fail, st, sm_count, s, launches);
+                        int sm_count, cudaStream_t s, int64_t* launches, const double* dt_dev) {
+    return ns == 9 ? chem_impl<9>(form, U, cs, idx, count, dt, dtc, rtol, atol, trial, fail, st, sm_count, s, launches,
+                                  dt_dev)
+                   : chem_impl<10>(form, U, cs, idx, count, dt, dtc, rtol, atol, trial, fail, st, sm_count, s, launches,
+                                   dt_dev);
 }
 cudaError_t launch_chem_commit(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, const double* trial,
                                cudaStream_t s, int64_t* launches) {

@@ -152,10 +152,11 @@ cudaError_t launch_stage_adjoint(int ns, const Level& L, const hf_patch& P, cons
                                  double* inbar, DevStatus* st, cudaStream_t s, int64_t* launches);
 size_t adjoint_bytes_per_cell(int ns, int ncalls, int K, int cap);
 cudaError_t launch_chem_adjoint(int ns, const AdjointArgs& a, cudaStream_t s, int64_t* launches);
+// dt_dev (nullable, plain form): read the interval from device memory instead of dt
 cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const int64_t* cell_index,
                         int64_t count, double dt, const double* dt_cell, double rtol, double atol,
                         double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
-                        int64_t* launches);
+                        int64_t* launches, const double* dt_dev = nullptr);
 // dt_dev (nullable): read the interval from device memory instead of dt
 cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
                                 const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,

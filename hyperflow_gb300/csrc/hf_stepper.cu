@@ -5,10 +5,10 @@
 // by discarding the work buffers (the reference clones the state, :413, :416).
 //
 // Two ways through a step:
-//  * graph path (batched chemistry, CFL dt): the whole Strang step - CFL reduction,
-//    dt on the device, four Euler stages (fused kernel, or ghost fill + face + update
-//    kernels of the plain form), ordered batched chemistry, validation - is one CUDA
-//    graph.  Every phase ORs its failure flags
+//  * graph path (CFL dt, either chemistry form): the whole Strang step - CFL
+//    reduction, dt on the device, four Euler stages (fused kernel, or ghost fill + face
+//    + update kernels of the plain form), the chemistry (ordered batched kernel, or one
+//    thread per cell), commit, validation - is one CUDA graph.  Every phase ORs its failure flags
 //    into one status block; the host reads it once per step.  Any flag discards the
 //    step and the host-controlled path below re-runs it.
 //  * host-controlled path: the ABI calls one by one with a status read after each,
@@ -171,12 +171,17 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     HF_Q(euler(S0, nullptr, T1));
     HF_Q(euler(T1, S0, X));
     HF_Q(phase_mark(st, rec, 1, s, nl));
-    // react(dt): work-queue head reset, then the ordered batched kernel, commit, validate
+    // react(dt): work-queue head reset, then the chemistry kernel of the stepper's form,
+    // commit, validate
     HF_Q(cudaMemsetAsync(&st->gst->counter, 0, sizeof(unsigned long long), s));
     if (st->chemistry) {
-        HF_Q(launch_chem_batched(st->ns, X, P.comp_stride, st->cells, nc, 0.0, st->ddt, nullptr, st->rtol, st->atol,
-                                 st->hist.h, st->hist.cost, st->order, st->bins, st->trial, st->fail, st->gst,
-                                 st->sm_count, s, nl));
+        if (st->chem_form == HF_CHEM_PLAIN)  // the drop-in form: one thread per cell
+            HF_Q(launch_chem(st->ns, HF_CHEM_PLAIN, X, P.comp_stride, st->cells, nc, 0.0, nullptr, st->rtol, st->atol,
+                             st->trial, st->fail, st->gst, st->sm_count, s, nl, st->ddt));
+        else
+            HF_Q(launch_chem_batched(st->ns, X, P.comp_stride, st->cells, nc, 0.0, st->ddt, nullptr, st->rtol,
+                                     st->atol, st->hist.h, st->hist.cost, st->order, st->bins, st->trial, st->fail,
+                                     st->gst, st->sm_count, s, nl));
         HF_Q(launch_chem_commit(st->ns, X, P.comp_stride, st->cells, nc, st->trial, s, nl));
         HF_Q(launch_validate(st->ns, P, X, 0, st->gst, s, nl));
     }
@@ -194,9 +199,7 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     return cudaSuccess;
 }
 
-bool graph_ready(const hf_stepper* st) {
-    return st->use_graph && (st->chem_form == HF_CHEM_PERSISTENT || !st->chemistry);
-}
+bool graph_ready(const hf_stepper* st) { return st->use_graph != 0; }
 
 // One step through the graph.  Returns HF_OK with the accepted dt, HF_ERR_INADMISSIBLE
 // with *dt = the graph's dt when the step must be re-run on the host-controlled path,

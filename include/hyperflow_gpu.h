@@ -445,8 +445,8 @@ HF_EXPORT hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void
  * whose graph raises a flag stops the batch on the device (the steps after it do nothing)
  * and is re-run with host control (first-order redo, rollback, dt halving) exactly as
  * hf_stepper_step would.  Same results as nsteps calls of hf_stepper_step with *dt = 0.
- * *steps_done (may be NULL) receives the steps completed, also on error.  A stepper
- * with the plain (one thread per cell) chemistry form runs hf_stepper_step nsteps times. */
+ * *steps_done (may be NULL) receives the steps completed, also on error.  Either
+ * chemistry form (batched, or plain: one thread per cell) runs inside the graphs. */
 HF_EXPORT hf_status hf_stepper_run(hf_stepper* st, int32_t nsteps, double cfl, int32_t* steps_done, void* stream);
 /* Copy the valid cells out, SoA [NV][ny][nx], to DEVICE memory. */
 HF_EXPORT hf_status hf_stepper_get(hf_stepper* st, double* U, void* stream);
@@ -456,8 +456,8 @@ HF_EXPORT hf_status hf_stepper_get_host(hf_stepper* st, double* U, void* stream)
 HF_EXPORT double hf_stepper_time(const hf_stepper* st);
 /* stableDt of the current state (BlockAMR.cpp:335-346). */
 HF_EXPORT hf_status hf_stepper_cfl_dt(hf_stepper* st, double cfl, double* dt, void* stream);
-/* Steps taken through the captured CUDA graph (either flux form + batched chemistry + CFL
- * dt: one graph launch and one status read per step) and through the host-controlled path
+/* Steps taken through the captured CUDA graph (either flux form + either chemistry form +
+ * CFL dt: one graph launch and one status read per step) and through the host-controlled path
  * (every other case, and any graph step whose status reported a failure, re-run from the
  * untouched start state).  Extension: the reference has no device graph. */
 HF_EXPORT void hf_stepper_stats(const hf_stepper* st, int64_t* graph_steps, int64_t* host_steps);

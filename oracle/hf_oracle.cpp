@@ -55,33 +55,89 @@ inline int EN() { return NS + 2; }
 constexpr int MAXV = NS_MAX + 3;
 constexpr double R = GAS_CONSTANT;
 
+// ---------------------------------------------------------------- flop counting
+// The thermo, UV inversion and kinetics functions below are templates on the scalar
+// type: the oracle runs them on double; on Fl they count their own floating-point work
+// (add, sub, mul, div, sqrt: one flop each; exp, log, log10, pow: transcendental calls,
+// counted apart), which gives the FP64 work of one right-hand side and one Jacobian
+// as this restatement does it.  Operations between constants (the mechanism's table
+// values) are folded at compile time and not counted.
+thread_local long g_fl_ops = 0, g_fl_trans = 0;
+struct Fl {
+    double v;
+    Fl() = default;
+    Fl(double x) : v(x) {}
+};
+inline Fl operator+(Fl a, Fl b) { ++g_fl_ops; return Fl(a.v + b.v); }
+inline Fl operator-(Fl a, Fl b) { ++g_fl_ops; return Fl(a.v - b.v); }
+inline Fl operator*(Fl a, Fl b) { ++g_fl_ops; return Fl(a.v * b.v); }
+inline Fl operator/(Fl a, Fl b) { ++g_fl_ops; return Fl(a.v / b.v); }
+inline Fl operator-(Fl a) { return Fl(-a.v); }
+inline Fl& operator+=(Fl& a, Fl b) { a = a + b; return a; }
+inline Fl& operator-=(Fl& a, Fl b) { a = a - b; return a; }
+inline Fl& operator*=(Fl& a, Fl b) { a = a * b; return a; }
+inline Fl& operator/=(Fl& a, Fl b) { a = a / b; return a; }
+inline bool operator<(Fl a, Fl b) { return a.v < b.v; }
+inline bool operator<=(Fl a, Fl b) { return a.v <= b.v; }
+inline bool operator>(Fl a, Fl b) { return a.v > b.v; }
+inline bool operator>=(Fl a, Fl b) { return a.v >= b.v; }
+inline double val(double x) { return x; }
+inline double val(Fl x) { return x.v; }
+inline double xexp(double x) { return std::exp(x); }
+inline double xlog(double x) { return std::log(x); }
+inline double xlog10(double x) { return std::log10(x); }
+inline double xpow(double x, double y) { return std::pow(x, y); }
+inline double xsqrt(double x) { return std::sqrt(x); }
+inline double xfabs(double x) { return std::fabs(x); }
+inline double xmax(double a, double b) { return std::max(a, b); }
+inline double xmin(double a, double b) { return std::min(a, b); }
+inline bool xfinite(double x) { return std::isfinite(x); }
+inline Fl xexp(Fl x) { ++g_fl_trans; return Fl(std::exp(x.v)); }
+inline Fl xlog(Fl x) { ++g_fl_trans; return Fl(std::log(x.v)); }
+inline Fl xlog10(Fl x) { ++g_fl_trans; return Fl(std::log10(x.v)); }
+inline Fl xpow(Fl x, Fl y) { ++g_fl_trans; return Fl(std::pow(x.v, y.v)); }
+inline Fl xsqrt(Fl x) { ++g_fl_ops; return Fl(std::sqrt(x.v)); }
+inline Fl xfabs(Fl x) { return Fl(std::fabs(x.v)); }
+inline Fl xmax(Fl a, Fl b) { return Fl(std::max(a.v, b.v)); }
+inline Fl xmin(Fl a, Fl b) { return Fl(std::min(a.v, b.v)); }
+inline bool xfinite(Fl x) { return std::isfinite(x.v); }
+// Newton iterations of the UV inversion when counting (a fixed count makes the flop
+// figure independent of the state): 0 = iterate to convergence
+thread_local int g_fixed_newton = 0;
+
 // ---------------------------------------------------------------- thermo
 const double* nasa(int k, double T) { return T <= T_MID[k] ? NASA_LOW[k] : NASA_HIGH[k]; }
-double cp_R(int k, double T) {
-    const double* a = nasa(k, T);
+template <class F>
+F cp_R(int k, F T) {
+    const double* a = nasa(k, val(T));
     return a[0] + T * (a[1] + T * (a[2] + T * (a[3] + T * a[4])));
 }
-double h_RT(int k, double T) {
-    const double* a = nasa(k, T);
+template <class F>
+F h_RT(int k, F T) {
+    const double* a = nasa(k, val(T));
     return a[0] + T * (a[1] / 2 + T * (a[2] / 3 + T * (a[3] / 4 + T * a[4] / 5))) + a[5] / T;
 }
-double s_R(int k, double T) {
-    const double* a = nasa(k, T);
-    return a[0] * std::log(T) + T * (a[1] + T * (a[2] / 2 + T * (a[3] / 3 + T * a[4] / 4))) + a[6];
+template <class F>
+F s_R(int k, F T) {
+    const double* a = nasa(k, val(T));
+    return a[0] * xlog(T) + T * (a[1] + T * (a[2] / 2 + T * (a[3] / 3 + T * a[4] / 4))) + a[6];
 }
 // specific internal energy and cv of a composition (mass fractions, not normalised)
-double mix_e(const double* Y, double T) {
-    double s = 0;
+template <class F>
+F mix_e(const F* Y, F T) {
+    F s = 0;
     for (int k = 0; k < NS; ++k) s += Y[k] / MW[k] * (h_RT(k, T) - 1.0);
     return R * T * s;
 }
-double mix_cv(const double* Y, double T) {
-    double s = 0;
+template <class F>
+F mix_cv(const F* Y, F T) {
+    F s = 0;
     for (int k = 0; k < NS; ++k) s += Y[k] / MW[k] * (cp_R(k, T) - 1.0);
     return R * s;
 }
-double inv_mmw(const double* Y) {
-    double s = 0;
+template <class F>
+F inv_mmw(const F* Y) {
+    F s = 0;
     for (int k = 0; k < NS; ++k) s += Y[k] / MW[k];
     return s;
 }
@@ -93,21 +149,25 @@ double inv_mmw(const double* Y) {
 // that jump has no root, and Newton then flips across T_mid with sub-kelvin steps:
 // two consecutive such flips return T_mid itself.  Returns false if it does not
 // converge in 60 iterations or leaves the finite positive range.
-bool solve_T(const double* Y, double e, double& T) {
-    if (!(T > 0) || !std::isfinite(T)) T = 1000.0;
+template <class F>
+bool solve_T(const F* Y, F e, F& T) {
+    if (!(T > 0) || !xfinite(T)) T = 1000.0;
     int flips = 0;
-    for (int it = 0; it < 60; ++it) {
-        double dT = (e - mix_e(Y, T)) / mix_cv(Y, T);
-        if (!std::isfinite(dT)) return false;
-        dT = std::min(1000.0, std::max(-1000.0, dT));
-        double Tn = T + dT;
+    const int fixed = g_fixed_newton;
+    for (int it = 0; it < (fixed > 0 ? fixed : 60); ++it) {
+        F dT = (e - mix_e(Y, T)) / mix_cv(Y, T);
+        if (!xfinite(dT)) return false;
+        dT = xmin(F(1000.0), xmax(F(-1000.0), dT));
+        F Tn = T + dT;
         if (Tn <= 0) Tn = 0.5 * T;
-        if (std::fabs(Tn - T) <= 1e-10 * Tn) { T = Tn; return true; }
-        flips = ((T <= 1000.0) != (Tn <= 1000.0) && std::fabs(Tn - T) < 0.5) ? flips + 1 : 0;
+        const bool converged = xfabs(Tn - T) <= 1e-10 * Tn;
+        if (fixed > 0) { T = Tn; continue; }
+        if (converged) { T = Tn; return true; }
+        flips = ((T <= 1000.0) != (Tn <= 1000.0) && xfabs(Tn - T) < 0.5) ? flips + 1 : 0;
         if (flips >= 2) { T = 1000.0; return true; }
         T = Tn;
     }
-    return false;
+    return fixed > 0;
 }
 
 double density(const double* q) {
@@ -174,38 +234,41 @@ double minmod1(double x, double y) {
 }
 
 // ---------------------------------------------------------------- kinetics
-struct Rates { double kf[NR], kr[NR], qf[NR], qr[NR]; };
+template <class F>
+struct RatesT { F kf[NR], kr[NR], qf[NR], qr[NR]; };
+using Rates = RatesT<double>;
 
 // Troe falloff factor F(T, Pr) and, optionally, d ln F / d ln Pr and d ln F / dT.
-double troe_F(const Reaction& rx, double T, double Pr, double* dlnF_dlnPr = nullptr, double* dlnF_dT = nullptr) {
-    const double e3 = std::exp(-T / rx.troeT3), e1 = std::exp(-T / rx.troeT1);
-    double Fcent = (1 - rx.troeA) * e3 + rx.troeA * e1;
-    double dFcent = -(1 - rx.troeA) / rx.troeT3 * e3 - rx.troeA / rx.troeT1 * e1;
+template <class F>
+F troe_F(const Reaction& rx, F T, F Pr, F* dlnF_dlnPr = nullptr, F* dlnF_dT = nullptr) {
+    const F e3 = xexp(-T / rx.troeT3), e1 = xexp(-T / rx.troeT1);
+    F Fcent = (1 - rx.troeA) * e3 + rx.troeA * e1;
+    F dFcent = -(1 - rx.troeA) / rx.troeT3 * e3 - rx.troeA / rx.troeT1 * e1;
     if (rx.hasT2) {
-        const double e2 = std::exp(-rx.troeT2 / T);
+        const F e2 = xexp(-rx.troeT2 / T);
         Fcent += e2;
         dFcent += rx.troeT2 / (T * T) * e2;
     }
     const bool fc_clamped = !(Fcent > 1e-300), pr_clamped = !(Pr > 1e-300);
-    const double lFc = std::log10(std::max(Fcent, 1e-300));
-    const double lPr = std::log10(std::max(Pr, 1e-300));
-    const double c = -0.4 - 0.67 * lFc, nn = 0.75 - 1.27 * lFc;
-    const double x = lPr + c, den = nn - 0.14 * x;
-    const double f1 = x / den;
-    const double g = 1 / (1 + f1 * f1);
-    const double lF = lFc * g;
+    const F lFc = xlog10(xmax(Fcent, F(1e-300)));
+    const F lPr = xlog10(xmax(Pr, F(1e-300)));
+    const F c = -0.4 - 0.67 * lFc, nn = 0.75 - 1.27 * lFc;
+    const F x = lPr + c, den = nn - 0.14 * x;
+    const F f1 = x / den;
+    const F g = 1 / (1 + f1 * f1);
+    const F lF = lFc * g;
     if (dlnF_dlnPr) {
         // d log10 F / d log10 Pr = lFc * (-2 f1 g^2) * df1/dx,  df1/dx = nn/den^2
-        *dlnF_dlnPr = pr_clamped ? 0.0 : lFc * (-2 * f1 * g * g) * (nn / (den * den));
+        *dlnF_dlnPr = pr_clamped ? F(0.0) : lFc * (-2 * f1 * g * g) * (nn / (den * den));
     }
     if (dlnF_dT) {
         // through Fcent: dx/dlFc = -0.67, dnn/dlFc = -1.27
-        const double df1 = (-0.67 * den - x * (-1.27 + 0.14 * 0.67)) / (den * den);
-        const double dlF_dlFc = g + lFc * (-2 * f1 * g * g) * df1;
-        const double dlFc_dT = fc_clamped ? 0.0 : dFcent / (Fcent * std::log(10.0));
+        const F df1 = (-0.67 * den - x * (-1.27 + 0.14 * 0.67)) / (den * den);
+        const F dlF_dlFc = g + lFc * (-2 * f1 * g * g) * df1;
+        const F dlFc_dT = fc_clamped ? F(0.0) : dFcent / (Fcent * std::log(10.0));
         *dlnF_dT = dlF_dlFc * dlFc_dT * std::log(10.0);
     }
-    return std::pow(10.0, lF);
+    return xpow(F(10.0), lF);
 }
 
 // Rate multipliers (sensitivity parameters p_r = ln multiplier_r): reaction r's
@@ -219,28 +282,29 @@ bool g_rate_mult_on = false;
 inline double rate_mult(int r) { return tl_rate_mult ? tl_rate_mult[r] : (g_rate_mult_on ? g_rate_mult[r] : 1.0); }
 
 // Rates of progress (kmol/m^3/s) at T and molar concentrations C.
-void progress(double T, const double* C, Rates& out) {
-    double g[NS_MAX];
+template <class F>
+void progress(F T, const F* C, RatesT<F>& out) {
+    F g[NS_MAX];
     for (int k = 0; k < NS; ++k) g[k] = h_RT(k, T) - s_R(k, T);
-    const double lnT = std::log(T), c0 = std::log(ONE_ATM / (R * T));
+    const F lnT = xlog(T), c0 = xlog(ONE_ATM / (R * T));
     for (int r = 0; r < NR; ++r) {
         const Reaction& rx = RXN[r];
-        double M = 0;
+        F M = 0;
         if (rx.type != RXN_ELEMENTARY) for (int k = 0; k < NS; ++k) M += rx.eff[k] * C[k];
-        double k = rx.A * rate_mult(r) * std::exp(rx.b * lnT - rx.EaR / T);
+        F k = rx.A * rate_mult(r) * xexp(rx.b * lnT - rx.EaR / T);
         if (rx.type == RXN_FALLOFF) {
-            const double k0 = rx.A0 * rate_mult(r) * std::exp(rx.b0 * lnT - rx.Ea0R / T);
-            const double Pr = k0 * M / k;
+            const F k0 = rx.A0 * rate_mult(r) * xexp(rx.b0 * lnT - rx.Ea0R / T);
+            const F Pr = k0 * M / k;
             k = k * (Pr / (1 + Pr)) * troe_F(rx, T, Pr);
         } else if (rx.type == RXN_THREE_BODY) {
             k *= M;
         }
-        double dG = 0;
+        F dG = 0;
         int dn = 0;
         for (int i = 0; i < rx.nprod; ++i) { dG += g[rx.prod[i]]; ++dn; }
         for (int i = 0; i < rx.nreac; ++i) { dG -= g[rx.reac[i]]; --dn; }
-        const double Kc = std::exp(-dG + dn * c0);
-        double qf = k, qr = k / Kc;
+        const F Kc = xexp(-dG + dn * c0);
+        F qf = k, qr = k / Kc;
         for (int i = 0; i < rx.nreac; ++i) qf *= C[rx.reac[i]];
         for (int i = 0; i < rx.nprod; ++i) qr *= C[rx.prod[i]];
         out.kf[r] = k;
@@ -250,12 +314,13 @@ void progress(double T, const double* C, Rates& out) {
     }
 }
 
-void net_production(double T, const double* C, double* wdot) {
-    Rates rt;
+template <class F>
+void net_production(F T, const F* C, F* wdot) {
+    RatesT<F> rt;
     progress(T, C, rt);
     for (int k = 0; k < NS; ++k) wdot[k] = 0;
     for (int r = 0; r < NR; ++r) {
-        const double q = rt.qf[r] - rt.qr[r];
+        const F q = rt.qf[r] - rt.qr[r];
         for (int i = 0; i < RXN[r].nreac; ++i) wdot[RXN[r].reac[i]] -= q;
         for (int i = 0; i < RXN[r].nprod; ++i) wdot[RXN[r].prod[i]] += q;
     }
@@ -264,26 +329,29 @@ void net_production(double T, const double* C, double* wdot) {
 // ---------------------------------------------------------------- chemistry ODE
 // chemistry.cpp:36-53: unknowns y = Y_0..Y_{NS-2}; the last species closes the
 // mass; rho and e are fixed; T is re-solved from e at every evaluation.
-struct ChemCell {
-    double rho, e, T;       // T is the warm start of the next UV solve
+template <class F>
+struct ChemCellT {
+    F rho, e, T;            // T is the warm start of the next UV solve
     long nrhs = 0, njac = 0;
 };
+using ChemCell = ChemCellT<double>;
 
-bool chem_rhs(ChemCell& c, const double* y, double* dy) {
+template <class F>
+bool chem_rhs(ChemCellT<F>& c, const F* y, F* dy) {
     const int n = NS - 1;
-    double Y[NS_MAX];
-    double s = 0;
+    F Y[NS_MAX];
+    F s = 0;
     for (int k = 0; k < n; ++k) { Y[k] = y[k]; s += y[k]; }
     Y[n] = 1 - s;
-    double T = c.T;
+    F T = c.T;
     if (!solve_T(Y, c.e, T)) return false;
     c.T = T;
-    double C[NS_MAX], w[NS_MAX];
+    F C[NS_MAX], w[NS_MAX];
     for (int k = 0; k < NS; ++k) C[k] = c.rho * Y[k] / MW[k];
     net_production(T, C, w);
     for (int k = 0; k < n; ++k) {
         dy[k] = w[k] * MW[k] / c.rho;
-        if (!std::isfinite(dy[k])) return false;
+        if (!xfinite(dy[k])) return false;
     }
     ++c.nrhs;
     return true;
@@ -310,88 +378,89 @@ bool chem_jac_fd(ChemCell& c, const double* y, const double* f0, double* J) {
 //   d(dy_i)/dy_j = W_i/rho * sum_r nu_ir [ sum_m dq_r/dC_m dC_m/dy_j + dq_r/dT dT/dy_j ]
 // where dC_m/dy_j = rho/W_j [m==j] - rho/W_last [m==last], and at fixed (rho, e)
 // dT/dy_j = -(e_j - e_last)/cv with e_k the species specific internal energies.
-bool chem_jac(ChemCell& c, const double* y, double* J) {
+template <class F>
+bool chem_jac(ChemCellT<F>& c, const F* y, F* J) {
     const int n = NS - 1, L = NS - 1;
-    double Y[NS_MAX];
-    double s = 0;
+    F Y[NS_MAX];
+    F s = 0;
     for (int k = 0; k < n; ++k) { Y[k] = y[k]; s += y[k]; }
     Y[n] = 1 - s;
-    double T = c.T;
+    F T = c.T;
     if (!solve_T(Y, c.e, T)) return false;
     c.T = T;
-    double C[NS_MAX];
+    F C[NS_MAX];
     for (int k = 0; k < NS; ++k) C[k] = c.rho * Y[k] / MW[k];
     // dq_r/dC_m and dq_r/dT
-    double dqdC[NR][NS_MAX], dqdT[NR];
-    double g[NS_MAX], dgdT[NS_MAX];
+    F dqdC[NR][NS_MAX], dqdT[NR];
+    F g[NS_MAX], dgdT[NS_MAX];
     for (int k = 0; k < NS; ++k) {
         g[k] = h_RT(k, T) - s_R(k, T);
         dgdT[k] = -h_RT(k, T) / T;  // d(g/RT)/dT = -h/(R T^2)
     }
-    const double lnT = std::log(T), c0 = std::log(ONE_ATM / (R * T));
+    const F lnT = xlog(T), c0 = xlog(ONE_ATM / (R * T));
     for (int r = 0; r < NR; ++r) {
         const Reaction& rx = RXN[r];
         for (int m = 0; m < NS; ++m) dqdC[r][m] = 0;
-        double M = 0;
+        F M = 0;
         if (rx.type != RXN_ELEMENTARY) for (int k = 0; k < NS; ++k) M += rx.eff[k] * C[k];
-        const double kinf = rx.A * rate_mult(r) * std::exp(rx.b * lnT - rx.EaR / T);
-        const double dlnkinf = rx.b / T + rx.EaR / (T * T);
-        double k = kinf, dkdT = kinf * dlnkinf, dkdM = 0;
+        const F kinf = rx.A * rate_mult(r) * xexp(rx.b * lnT - rx.EaR / T);
+        const F dlnkinf = rx.b / T + rx.EaR / (T * T);
+        F k = kinf, dkdT = kinf * dlnkinf, dkdM = 0;
         if (rx.type == RXN_THREE_BODY) {
             dkdM = kinf;
             k = kinf * M;
             dkdT = dkdT * M;
         } else if (rx.type == RXN_FALLOFF) {
-            const double k0 = rx.A0 * rate_mult(r) * std::exp(rx.b0 * lnT - rx.Ea0R / T);
-            const double dlnk0 = rx.b0 / T + rx.Ea0R / (T * T);
-            const double Pr = k0 * M / kinf;
-            double dlnF_dlnPr = 0, dlnF_dT = 0;
-            const double F = troe_F(rx, T, Pr, &dlnF_dlnPr, &dlnF_dT);
+            const F k0 = rx.A0 * rate_mult(r) * xexp(rx.b0 * lnT - rx.Ea0R / T);
+            const F dlnk0 = rx.b0 / T + rx.Ea0R / (T * T);
+            const F Pr = k0 * M / kinf;
+            F dlnF_dlnPr = 0, dlnF_dT = 0;
+            const F Ft = troe_F(rx, T, Pr, &dlnF_dlnPr, &dlnF_dT);
             // ln k = ln kinf + ln Pr - ln(1+Pr) + ln F(T, Pr)
-            const double dlnk_dlnPr = 1 - Pr / (1 + Pr) + dlnF_dlnPr;
-            k = kinf * Pr / (1 + Pr) * F;
-            const double dlnPr_dT = dlnk0 - dlnkinf;
+            const F dlnk_dlnPr = 1 - Pr / (1 + Pr) + dlnF_dlnPr;
+            k = kinf * Pr / (1 + Pr) * Ft;
+            const F dlnPr_dT = dlnk0 - dlnkinf;
             dkdT = k * (dlnkinf + dlnk_dlnPr * dlnPr_dT + dlnF_dT);
-            dkdM = M > 0 ? k * dlnk_dlnPr / M : k0 * F;  // limit M->0: k ~ k0*M*F
+            dkdM = M > 0 ? k * dlnk_dlnPr / M : k0 * Ft;  // limit M->0: k ~ k0*M*F
         }
-        double dG = 0, dGdT = 0;
+        F dG = 0, dGdT = 0;
         int dn = 0;
         for (int i = 0; i < rx.nprod; ++i) { dG += g[rx.prod[i]]; dGdT += dgdT[rx.prod[i]]; ++dn; }
         for (int i = 0; i < rx.nreac; ++i) { dG -= g[rx.reac[i]]; dGdT -= dgdT[rx.reac[i]]; --dn; }
-        const double Kc = std::exp(-dG + dn * c0);
-        const double dlnKc = -dGdT - dn / T;
-        double Pf = 1, Pr_ = 1;
+        const F Kc = xexp(-dG + dn * c0);
+        const F dlnKc = -dGdT - dn / T;
+        F Pf = 1, Pr_ = 1;
         for (int i = 0; i < rx.nreac; ++i) Pf *= C[rx.reac[i]];
         for (int i = 0; i < rx.nprod; ++i) Pr_ *= C[rx.prod[i]];
-        const double kr = k / Kc;
+        const F kr = k / Kc;
         // mass-action derivatives: d/dC_m of prod C over the list = sum over occurrences
         for (int i = 0; i < rx.nreac; ++i) {
-            double p = k;
+            F p = k;
             for (int j = 0; j < rx.nreac; ++j) if (j != i) p *= C[rx.reac[j]];
             dqdC[r][rx.reac[i]] += p;
         }
         for (int i = 0; i < rx.nprod; ++i) {
-            double p = kr;
+            F p = kr;
             for (int j = 0; j < rx.nprod; ++j) if (j != i) p *= C[rx.prod[j]];
             dqdC[r][rx.prod[i]] -= p;
         }
         if (rx.type != RXN_ELEMENTARY) {
-            const double net_over_k = Pf - Pr_ / Kc;  // q = k * net_over_k
+            const F net_over_k = Pf - Pr_ / Kc;  // q = k * net_over_k
             for (int m = 0; m < NS; ++m) dqdC[r][m] += dkdM * rx.eff[m] * net_over_k;
         }
         dqdT[r] = dkdT * Pf - (dkdT - k * dlnKc) / Kc * Pr_;
     }
     // dT/dy_j
-    double ek[NS_MAX];
+    F ek[NS_MAX];
     for (int k2 = 0; k2 < NS; ++k2) ek[k2] = R * T / MW[k2] * (h_RT(k2, T) - 1.0);
-    const double cv = mix_cv(Y, T);
-    double dTdy[NS_MAX];
+    const F cv = mix_cv(Y, T);
+    F dTdy[NS_MAX];
     for (int j = 0; j < n; ++j) dTdy[j] = -(ek[j] - ek[L]) / cv;
     // dw_i/dy_j
     for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) J[i * n + j] = 0;
     for (int r = 0; r < NR; ++r) {
         const Reaction& rx = RXN[r];
-        double dq[NS_MAX];
+        F dq[NS_MAX];
         for (int j = 0; j < n; ++j)
             dq[j] = dqdC[r][j] * c.rho / MW[j] - dqdC[r][L] * c.rho / MW[L] + dqdT[r] * dTdy[j];
         for (int i = 0; i < rx.nreac; ++i) {
@@ -596,8 +665,10 @@ ChemResult rodas4(ChemCell& c, double* y, double dt, double rtol, double atol, l
     return rosenbrock(sys, NS - 1, y, dt, rtol, atol, max_steps, 0.0, 0);
 }
 
-// chemistry.cpp:55-76 on one cell (AoS state of NV doubles).
-int chem_advance(double* u, double dt, double rtol, double atol, long max_steps, long* steps_out) {
+// chemistry.cpp:55-76 on one cell (AoS state of NV doubles).  steps_out: attempts
+// (accepted + rejected); accepted_out (optional): accepted steps.
+int chem_advance(double* u, double dt, double rtol, double atol, long max_steps, long* steps_out,
+                 long* accepted_out = nullptr) {
     if (!(dt > 0) || !std::isfinite(dt)) return CHEM_FAIL;
     Props pr;
     if (!properties(u, pr, 1000.0)) return CHEM_FAIL;
@@ -610,6 +681,7 @@ int chem_advance(double* u, double dt, double rtol, double atol, long max_steps,
     for (int k = 0; k < n; ++k) y[k] = u[k] / c.rho;
     ChemResult r = rodas4(c, y, dt, rtol, atol, max_steps);
     if (steps_out) *steps_out = r.steps + r.rejected;
+    if (accepted_out) *accepted_out = r.steps;
     if (r.status != CHEM_OK) return r.status;
     double s = 0;
     for (int k = 0; k < n; ++k) {
@@ -884,6 +956,47 @@ int64_t or_chem_batch(double* U, int64_t count, double dt, const double* dt_cell
     for (int64_t k = 0; k < count; ++k) if (fail[k]) return k;
     std::copy(trial.begin(), trial.end(), U);
     return -1;
+}
+
+// Accepted and rejected Rodas4 steps per cell of a batch (U is not changed); cells
+// that fail report -1 accepted steps.
+void or_chem_batch_stats(const double* U, int64_t count, double dt, const double* dt_cell, double rtol, double atol,
+                         int threads, long* accepted, long* rejected) {
+    const int nv = NV();
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < count; ++k) {
+        double u[MAXV];
+        std::copy(U + k * nv, U + (k + 1) * nv, u);
+        long att = 0, acc = 0;
+        const int st = chem_advance(u, dt_cell ? dt_cell[k] : dt, rtol, atol, 5000, &att, &acc);
+        accepted[k] = st == CHEM_OK ? acc : -1;
+        rejected[k] = att - acc;
+    }
+}
+
+// FP64 work of one right-hand side and one analytic Jacobian of the chemistry ODE at
+// (rho, e, y) with the UV inversion taking exactly `newton` iterations from T: out[0]
+// flops and out[1] transcendental calls of the RHS, out[2] and out[3] of the Jacobian.
+void or_chem_flops(double rho, double e, const double* y, double T, int newton, double* out) {
+    const int n = NS - 1;
+    ChemCellT<Fl> c;
+    c.rho = rho;
+    c.e = e;
+    Fl yy[NS_MAX], f[NS_MAX], J[NS_MAX * NS_MAX];
+    for (int k = 0; k < n; ++k) yy[k] = y[k];
+    g_fixed_newton = newton;
+    for (int which = 0; which < 2; ++which) {
+        c.T = T;
+        g_fl_ops = g_fl_trans = 0;
+        if (which == 0) chem_rhs(c, yy, f);
+        else chem_jac(c, yy, J);
+        out[2 * which] = (double)g_fl_ops;
+        out[2 * which + 1] = (double)g_fl_trans;
+    }
+    g_fixed_newton = 0;
 }
 
 // Objective (OBJ_*) of count AoS cells over nsub adaptive chemistry calls of dt

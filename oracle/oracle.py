@@ -62,6 +62,9 @@ def lib():
         L.or_chem_rhs.argtypes = [ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
         L.or_chem_jac.argtypes = [ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, ctypes.c_int]
         L.or_chem_advance.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_long, _lp]
+        L.or_chem_batch_stats.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_int, _lp, _lp]
+        L.or_chem_flops.argtypes = [ctypes.c_double, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_int, _dp]
         L.or_chem_batch.restype = ctypes.c_int64
         L.or_chem_batch.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int, _lp]
@@ -209,6 +212,33 @@ def chem_batch(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
 
 
 OBJECTIVES = {"ignition_delay": 0, "peak_pressure": 1, "final_T": 2}
+
+
+def chem_batch_stats(U, dt, rtol=1e-8, atol=1e-15, threads=0, dt_cell=None):
+    """Accepted and rejected Rodas4 steps per cell of a (count, NV) AoS batch advanced
+    over dt (or dt_cell per cell); -1 accepted marks a failed cell.  U is unchanged."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    n = U.shape[0]
+    acc, rej = np.zeros(n, np.int64), np.zeros(n, np.int64)
+    dtc = None if dt_cell is None else np.ascontiguousarray(dt_cell, dtype=np.float64)
+    lib().or_chem_batch_stats(_p(U), n, float(dt), _p(dtc) if dtc is not None else None, float(rtol), float(atol),
+                              int(threads), acc.ctypes.data_as(_lp), rej.ctypes.data_as(_lp))
+    return acc, rej
+
+
+def chem_flops(u, newton=3):
+    """FP64 flops and transcendental calls of one chemistry right-hand side and one
+    analytic Jacobian at the AoS state u, the UV inversion fixed at `newton` iterations
+    from the state's own temperature: (rhs_flops, rhs_trans, jac_flops, jac_trans)."""
+    u = np.asarray(u, dtype=np.float64)
+    ns = nspecies()
+    rho = float(u[:ns].sum())
+    e = float(u[ns + 2] / rho - 0.5 * ((u[ns] / rho) ** 2 + (u[ns + 1] / rho) ** 2))
+    T = float(properties(u[None, :])[2][0])
+    y = np.ascontiguousarray(u[:ns - 1] / rho)
+    out = np.zeros(4)
+    lib().or_chem_flops(rho, e, _p(y), T, int(newton), _p(out))
+    return tuple(out)
 
 
 def set_flux_threads(threads=1):

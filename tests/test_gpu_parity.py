@@ -340,16 +340,17 @@ def test_strang_step_matches_oracle(gpu, oracle):
         s.close()
 
 
-@pytest.mark.parametrize("flux", ["fused", "plain"])
-def test_graph_step_equals_host_step(gpu, flux):
+@pytest.mark.parametrize("flux,chem", [("fused", "batched"), ("plain", "batched"), ("plain", "plain")])
+def test_graph_step_equals_host_step(gpu, flux, chem):
     """The CUDA-graph Strang step (device dt, one status read per step) gives the same
-    states, bit for bit, as the host-controlled path on the same inputs."""
+    states, bit for bit, as the host-controlled path on the same inputs, with either
+    chemistry form inside the graph."""
     import hyperflow_gb300 as hf
     from hyperflow_gb300 import workloads as W
     U, lvd = W.det2d(seed=2, diluent="N2", nx=96, ny=24, hot_columns=8)
     lv = hf.make_level(**lvd)
-    a = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem="batched")
-    b = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem="batched")
+    a = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem=chem)
+    b = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem=chem)
     b.set_graph(False)
     for _ in range(3):
         da = a.step(cfl=0.5)
@@ -360,8 +361,10 @@ def test_graph_step_equals_host_step(gpu, flux):
     assert a.time == b.time
 
 
-@pytest.mark.parametrize("flux,cfl", [("fused", 0.5), ("fused", 8.0), ("plain", 0.5), ("plain", 8.0)])
-def test_device_resident_run_equals_steps(gpu, flux, cfl):
+@pytest.mark.parametrize("flux,cfl,chem", [("fused", 0.5, "batched"), ("fused", 8.0, "batched"),
+                                          ("plain", 0.5, "batched"), ("plain", 8.0, "batched"),
+                                          ("plain", 0.5, "plain"), ("plain", 8.0, "plain")])
+def test_device_resident_run_equals_steps(gpu, flux, cfl, chem):
     """hf_stepper_run (graph steps launched back to back, one record read per batch)
     gives the states, times and step kinds of the same number of step() calls.  At CFL
     8 graph steps fail: the run stops on the device at the failed step and re-runs it
@@ -370,8 +373,8 @@ def test_device_resident_run_equals_steps(gpu, flux, cfl):
     from hyperflow_gb300 import workloads as W
     U, lvd = W.det2d(seed=3, diluent="N2", nx=96, ny=24, hot_columns=8)
     lv = hf.make_level(**lvd)
-    a = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem="batched")
-    b = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem="batched")
+    a = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem=chem)
+    b = hf.Stepper(gpu, lv, cuda(U), flux=flux, chem=chem)
     assert a.run(5, cfl=cfl) == 5
     for _ in range(5):
         b.step(cfl=cfl)
