@@ -38,7 +38,8 @@ class Patch(ctypes.Structure):
 
 class Counters(ctypes.Structure):
     _fields_ = [("first_order_stages", _i64), ("roundoff_repairs", _i64), ("retries", _i64),
-                ("chem_cell_calls", _i64), ("chem_steps", _i64), ("kernel_launches", _i64)]
+                ("chem_cell_calls", _i64), ("chem_steps", _i64), ("kernel_launches", _i64),
+                ("chem_coop_cells", _i64)]
 
 
 class ChemHistory(ctypes.Structure):

@@ -159,6 +159,7 @@ void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries) 
     ctx->cnt.retries += retries;
 }
 void ctx_add_repairs(hf_ctx* ctx, int64_t repairs) { ctx->cnt.roundoff_repairs += repairs; }
+void ctx_add_coop(hf_ctx* ctx, int64_t coop_cells) { ctx->cnt.chem_coop_cells += coop_cells; }
 void ctx_set_error(hf_ctx* ctx, const char* msg) {
     if (ctx) ctx->err = msg;
 }
@@ -528,7 +529,7 @@ static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const 
     const size_t b_trial = sizeof(double) * (size_t)nv * count;
     const size_t b_fail = (sizeof(int) * (size_t)count + 15) & ~size_t(15);
     const size_t b_order = (sizeof(int32_t) * (size_t)count + 15) & ~size_t(15);
-    char* w = static_cast<char*>(scratch(ctx, b_trial + b_fail + b_order + 16 * sizeof(unsigned long long)));
+    char* w = static_cast<char*>(scratch(ctx, b_trial + b_fail + b_order + CHEM_BINS * sizeof(unsigned long long)));
     if (!w) return fail(ctx, HF_ERR_CUDA, "chem_advance: scratch allocation failed");
     double* trial = reinterpret_cast<double*>(w);
     int* failv = reinterpret_cast<int*>(w + b_trial);
@@ -547,6 +548,7 @@ static hf_status chem_common(hf_ctx* ctx, double* U, int64_t comp_stride, const 
     toc(ctx, s, ctx->cnt.kernel_launches - l0);
     HF_CUDA(read_status(ctx, s));
     ctx->cnt.chem_steps += (int64_t)ctx->st_host->steps;
+    ctx->cnt.chem_coop_cells += (int64_t)ctx->st_host->coop_cells;
     const unsigned f = ctx->st_host->flags;
     if (f & (ST_CHEM_FAIL | ST_MAXSTEPS)) {
         if (first_failed) *first_failed = (int64_t)ctx->st_host->bad_cell;
@@ -656,6 +658,7 @@ static hf_status chem_sensitivity(hf_ctx* ctx, const double* U0, int64_t comp_st
     if (e != cudaSuccess) return cuda_fail(ctx, e, "chem_adjoint launch");
     HF_CUDA(read_status(ctx, s));
     ctx->cnt.chem_steps += (int64_t)ctx->st_host->steps;
+    ctx->cnt.chem_coop_cells += (int64_t)ctx->st_host->coop_cells;
     const unsigned f = ctx->st_host->flags;
     if (f & (ST_CHEM_FAIL | ST_MAXSTEPS)) {
         if (first_failed) *first_failed = (int64_t)ctx->st_host->bad_cell;

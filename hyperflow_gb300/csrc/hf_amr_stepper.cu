@@ -515,7 +515,7 @@ cudaError_t g_react(hf_amr* m, double* const* X, cudaStream_t s, int64_t* nl) {
     for (int l = 0; e == cudaSuccess && l <= m->finest; ++l) {
         AmrLevel& a = m->lev[l];
         if (!a.nleaf) continue;
-        e = cudaMemsetAsync(&m->gst->counter, 0, sizeof(unsigned long long), s);  // work-queue head
+        e = cudaMemsetAsync(&m->gst->counter, 0, 2 * sizeof(unsigned long long), s);  // work-queue heads
         if (e == cudaSuccess)
             e = hf::launch_chem_batched(m->ns, X[l], a.dom.comp_stride, a.cells, a.nleaf, 0.0, m->ddt, nullptr,
                                         m->o.rtol, m->o.atol, a.hist.h, a.hist.cost, a.order, a.bins, a.trial, a.fail,
@@ -557,7 +557,7 @@ hf_status g_alloc(hf_amr* m) {
         if (cudaMalloc(&a.trial, sizeof(double) * m->nv * nc) != cudaSuccess ||
             cudaMalloc(&a.fail, sizeof(int) * nc) != cudaSuccess ||
             cudaMalloc(&a.order, sizeof(int32_t) * nc) != cudaSuccess ||
-            cudaMalloc(&a.bins, 16 * sizeof(unsigned long long)) != cudaSuccess)
+            cudaMalloc(&a.bins, hf::CHEM_BINS * sizeof(unsigned long long)) != cudaSuccess)
             return HF_ERR_CUDA;
     }
     return HF_OK;
@@ -616,6 +616,7 @@ hf_status g_step(hf_amr* m, double cfl, double* dt, cudaStream_t s) {
     int64_t leaf = 0;
     for (int l = 0; l <= m->finest; ++l) leaf += m->lev[l].nleaf;
     hf::ctx_add_launches(m->ctx, m->graph_kernels[k], m->o.chemistry ? leaf : 0, (int64_t)m->gst_host->steps);
+    hf::ctx_add_coop(m->ctx, (int64_t)m->gst_host->coop_cells);
     *dt = m->ddt_host[0];
     return m->gst_host->flags ? HF_ERR_INADMISSIBLE : HF_OK;
 }

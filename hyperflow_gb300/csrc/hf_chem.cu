@@ -18,7 +18,7 @@
 // compile-time constants of the generated mechanism table, so every species index
 // is a register index.
 #include <cstdlib>
-#include "hf_kinetics.cuh"
+#include "hf_chem_coop.cuh"
 
 namespace hf {
 
@@ -141,6 +141,89 @@ __global__ void k_chem_commit(double* __restrict__ U, int64_t cs, const int64_t*
 // queue ordered most-expensive-first (order[]), starting each cell with
 // cell_begin_batched, and recording per cell the attempts taken (cost[]) and the
 // controller's proposed next step (h_hist[]) for the next call.
+// Cooperative phase of the batched kernel: queue positions [0, ncoop) (the costliest
+// buckets), one cell per group of 8 lanes (hf_chem_coop.cuh), the refill scheme of the
+// per-lane loop with groups in place of lanes.
+template <int NS>
+__device__ __forceinline__ void coop_phase(const double* __restrict__ U, int64_t cs,
+                                           const int64_t* __restrict__ cell_index, const int32_t* __restrict__ order,
+                                           int64_t count, int64_t ncoop, double dt, const double* __restrict__ dt_cell,
+                                           double rtol, double atol, double* __restrict__ trial,
+                                           int* __restrict__ fail, double* __restrict__ h_hist,
+                                           int32_t* __restrict__ cost, DevStatus* st, coop::GShared* sh) {
+    using namespace coop;
+    const Grp g = grp();
+    const unsigned lane = threadIdx.x & 31;
+    GInt c{};
+    double y = 0.0, f0 = 0.0, J[NQ];
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) J[j] = 0.0;
+    int64_t cell = -1;
+    bool active = false, drained = false;
+    unsigned long long my_attempts = 0;
+    auto finish = [&](int64_t k, bool screened) {
+        double u[NS + 3];
+        const bool ok = gend<NS>(g, c, y, u, sh->T);
+        if (g.t == 0) {
+            if (ok) {
+#pragma unroll
+                for (int n = 0; n < NS + 3; ++n) trial[n * count + k] = u[n];
+                fail[k] = 0;
+                if (!screened && h_hist) h_hist[k] = c.h;
+                if (cost) cost[k] = screened ? 0 : c.attempts;
+            } else {
+                report(st, fail, k, CELL_FAIL);
+            }
+        }
+    };
+    for (;;) {
+        if (!drained) {
+            const unsigned need = __ballot_sync(0xffffffffu, !active) & 0x01010101u;  // first lane of each group
+            bool none = false;
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                unsigned long long base = 0;
+                if ((int)lane == leader) base = atomicAdd(&st->coop_counter, (unsigned long long)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!active) {
+                    const int64_t q = (int64_t)(base + __popc(need & ((1u << g.base) - 1u)));
+                    if (q < ncoop) {
+                        const int64_t k = (int64_t)order[q];
+                        cell = k;
+                        double u[NS + 3];
+                        const int64_t b = cell_index ? cell_index[k] : k;
+#pragma unroll
+                        for (int n = 0; n < NS + 3; ++n) u[n] = U[b + n * cs];
+                        const int r = gbegin<NS>(g, c, y, f0, J, u, dt_cell ? dt_cell[k] : dt, rtol, atol,
+                                                 h_hist ? h_hist[k] : 0.0, sh);
+                        if (g.t == 0) atomicAdd(&st->coop_cells, 1ull);
+                        if (r == CELL_CONTINUE) active = true;
+                        else if (r == CELL_DONE) finish(k, true);
+                        else if (g.t == 0) report(st, fail, k, CELL_FAIL);
+                    } else {
+                        none = true;
+                    }
+                }
+            }
+            drained = __any_sync(0xffffffffu, none);
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (drained) break;
+            continue;
+        }
+        if (active) {
+            const int r = gattempt<NS>(g, c, y, f0, J, rtol, atol, sh);
+            if (r != CELL_CONTINUE) {
+                if (g.t == 0) my_attempts += c.attempts;
+                if (r == CELL_DONE) finish(cell, false);
+                else if (g.t == 0) report(st, fail, cell, r == CELL_MAXSTEPS ? CELL_MAXSTEPS : CELL_FAIL);
+                active = false;
+            }
+        }
+    }
+    if (my_attempts) atomicAdd(&st->steps, my_attempts);
+}
+
 template <int NS, int MINB>
 __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restrict__ U, int64_t cs,
                                                      const int64_t* __restrict__ cell_index,
@@ -149,10 +232,17 @@ __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restr
                                                      const double* __restrict__ dt_cell, double rtol, double atol,
                                                      double* __restrict__ trial, int* __restrict__ fail,
                                                      double* __restrict__ h_hist, int32_t* __restrict__ cost,
-                                                     DevStatus* st) {
+                                                     const unsigned long long* __restrict__ coop_n, DevStatus* st) {
     if (st->abort_run) return;  // an earlier step of this device-resident run failed
     const unsigned lane = threadIdx.x & 31;
     if (dt_dev) dt = *dt_dev;  // interval from device memory (graph-captured steps)
+    // the costliest cells first, one cell per group of 8 lanes; the rest one per lane
+    const int64_t ncoop = (order && coop_n) ? (int64_t)*coop_n : 0;
+    if (ncoop > 0) {
+        __shared__ coop::GShared sh[2][4];  // 64-thread blocks: 2 warps of 4 groups
+        coop_phase<NS>(U, cs, cell_index, order, count, ncoop, dt, dt_cell, rtol, atol, trial, fail, h_hist, cost,
+                       st, &sh[threadIdx.x >> 5][(threadIdx.x & 31) >> 3]);
+    }
     ChemCell<NS> c;
     int64_t cell = -1;
     bool active = false, drained = false;
@@ -167,7 +257,7 @@ __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restr
                 if ((int)lane == leader) base = atomicAdd(&st->counter, (unsigned long long)__popc(need));
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (!active) {
-                    const int64_t q = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
+                    const int64_t q = ncoop + (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
                     if (q < count) {
                         const int64_t k = order ? (int64_t)order[q] : q;
                         cell = k;
@@ -234,14 +324,21 @@ __global__ void k_order_hist(const int32_t* __restrict__ cost, int64_t count, un
     __syncthreads();
     if (threadIdx.x < NBUCKET && sb[threadIdx.x]) atomicAdd(&bins[threadIdx.x], (unsigned long long)sb[threadIdx.x]);
 }
-__global__ void k_order_scan(unsigned long long* bins) {
-    // bins[b] -> start offset of bucket b, descending buckets first
-    unsigned long long off = 0;
+// bins[b] -> start offset of bucket b, descending buckets first; bins[NBUCKET] = the
+// cells of the cooperative queue: whole buckets from the costliest down to min_bucket
+// while they fit in cap cells (whole buckets, so the choice does not depend on the
+// order within a bucket).
+__global__ void k_order_scan(unsigned long long* bins, unsigned long long cap, int min_bucket) {
+    unsigned long long off = 0, ncoop = 0;
+    bool open = true;
     for (int b = NBUCKET - 1; b >= 0; --b) {
         const unsigned long long n = bins[b];
+        if (open && b >= min_bucket && ncoop + n <= cap) ncoop += n;
+        else open = false;
         bins[b] = off;
         off += n;
     }
+    bins[NBUCKET] = ncoop;
 }
 __global__ void k_order_scatter(const int32_t* __restrict__ cost, int64_t count, unsigned long long* __restrict__ bins,
                                 int32_t* __restrict__ order) {
@@ -257,23 +354,21 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
                                      double* h_hist, int32_t* cost, int32_t* order, unsigned long long* bins,
                                      double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
                                      int64_t* launches) {
-    if (cost && order) {
-        cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * NBUCKET, s);
-        if (e != cudaSuccess) return e;
-        const int g = sm_count * 4;
-        k_order_hist<<<g, 256, 0, s>>>(cost, count, bins);
-        k_order_scan<<<1, 1, 0, s>>>(bins);
-        k_order_scatter<<<g, 256, 0, s>>>(cost, count, bins, order);
-        *launches += 3;
-    } else {
-        order = nullptr;
-    }
     // register budget of the queue kernel: 255 (4 blocks of 64 per SM) or 128 (8 blocks);
     // HF_CHEM_MINB=8 selects the second.  Both run the same per-cell code.
     static const int minb = [] {
         const char* e = getenv("HF_CHEM_MINB");
         const int v = e ? atoi(e) : 4;
         return (v == 5 || v == 6 || v == 8) ? v : 4;
+    }();
+    // cooperative queue: cells that took at least 2^min_bucket - 1 attempts in the
+    // previous call (HF_COOP_MIN_BUCKET, default 5; HF_COOP=0 turns the phase off)
+    static const int coop_min = [] {
+        const char* off = getenv("HF_COOP");
+        if (off && atoi(off) == 0) return NBUCKET;
+        const char* e = getenv("HF_COOP_MIN_BUCKET");
+        const int v = e ? atoi(e) : 5;
+        return v < 1 ? 1 : (v > NBUCKET ? NBUCKET : v);
     }();
     auto kern = minb == 8   ? k_chem_batched<NS, 8>
                 : minb == 6 ? k_chem_batched<NS, 6>
@@ -287,8 +382,22 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
     const int64_t need = (count + bs - 1) / bs;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
+    const unsigned long long* coop_n = nullptr;
+    if (cost && order) {
+        cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * (NBUCKET + 1), s);
+        if (e != cudaSuccess) return e;
+        const int g = sm_count * 4;
+        const unsigned long long cap = (unsigned long long)blocks * (bs / 32) * 4;  // 4 groups per warp
+        k_order_hist<<<g, 256, 0, s>>>(cost, count, bins);
+        k_order_scan<<<1, 1, 0, s>>>(bins, cap, coop_min);
+        k_order_scatter<<<g, 256, 0, s>>>(cost, count, bins, order);
+        *launches += 3;
+        coop_n = bins + NBUCKET;
+    } else {
+        order = nullptr;
+    }
     kern<<<(unsigned)blocks, bs, 0, s>>>(U, cs, idx, order, count, dt, dt_dev, dtc, rtol, atol, trial, fail, h_hist,
-                                         cost, st);
+                                         cost, coop_n, st);
     ++*launches;
     return cudaGetLastError();
 }

@@ -13,11 +13,13 @@ struct DevStatus {
     unsigned long long bad_cell;   // lowest failing linear index (atomicMin), ~0 = none
     unsigned long long rate_bits;  // CFL: max rate as the bits of a non-negative double
     unsigned long long counter;    // work-queue head / generic counter
+    unsigned long long coop_counter;  // head of the batched chemistry's cooperative queue
     unsigned long long steps;      // integrator steps (accepted + rejected)
     double deficit[16];            // roundoff repair deficits per species
     unsigned long long peak_bits[16];
     unsigned long long donor[16];
     unsigned long long repairs;
+    unsigned long long coop_cells;  // cells the batched chemistry took in groups of 8 lanes
     // Set when a step of a device-resident multi-step run failed; the step kernels of
     // the later steps of that run return at entry.  Never set outside such runs (the
     // per-step reset of the status block leaves it alone: it is the last member).
@@ -54,6 +56,7 @@ inline Level make_level(const hf_level& l) {
 // Counter updates from the host stepper (hf_abi.cu)
 void ctx_add_counters(hf_ctx* ctx, int64_t first_order_stages, int64_t retries);
 void ctx_add_repairs(hf_ctx* ctx, int64_t repairs);
+void ctx_add_coop(hf_ctx* ctx, int64_t coop_cells);
 // The message hf_last_error returns, for failures found outside hf_abi.cu
 void ctx_set_error(hf_ctx* ctx, const char* msg);
 // Counters and device time of work run outside the ABI entry points (graph-captured steps)
@@ -158,6 +161,9 @@ cudaError_t launch_chem(int ns, int form, double* U, int64_t comp_stride, const 
                         double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
                         int64_t* launches, const double* dt_dev = nullptr);
 // dt_dev (nullable): read the interval from device memory instead of dt
+// bins: CHEM_BINS unsigned long long of device scratch (cost buckets and the size of the
+// cooperative queue)
+constexpr int CHEM_BINS = 32;
 cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
                                 const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,
                                 int32_t* cost, int32_t* order, unsigned long long* bins, double* trial, int* fail,

@@ -36,6 +36,7 @@ struct RunRec {
     double dt[RUN_CAP];
     unsigned int flags[RUN_CAP];
     unsigned long long steps[RUN_CAP];   // chemistry step attempts
+    unsigned long long coop[RUN_CAP];    // cells of the cooperative chemistry queue
     unsigned long long t[RUN_CAP][4];    // %globaltimer at the phase boundaries (ns)
 };
 }  // namespace
@@ -127,6 +128,7 @@ __global__ void k_run_record(hf::DevStatus* st, const double* ddt, RunRec* rec) 
         rec->dt[n] = ddt[0];
         rec->flags[n] = st->flags;
         rec->steps[n] = st->steps;
+        rec->coop[n] = st->coop_cells;
     }
     rec->n = n + 1;
     if (st->flags) st->abort_run = 1;
@@ -173,7 +175,7 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     HF_Q(phase_mark(st, rec, 1, s, nl));
     // react(dt): work-queue head reset, then the chemistry kernel of the stepper's form,
     // commit, validate
-    HF_Q(cudaMemsetAsync(&st->gst->counter, 0, sizeof(unsigned long long), s));
+    HF_Q(cudaMemsetAsync(&st->gst->counter, 0, 2 * sizeof(unsigned long long), s));  // work-queue heads
     if (st->chemistry) {
         if (st->chem_form == HF_CHEM_PLAIN)  // the drop-in form: one thread per cell
             HF_Q(launch_chem(st->ns, HF_CHEM_PLAIN, X, P.comp_stride, st->cells, nc, 0.0, nullptr, st->rtol, st->atol,
@@ -255,6 +257,7 @@ hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
         return HF_ERR_CUDA;
     hf::ctx_add_launches(st->ctx, st->graph_kernels[k], st->chemistry ? (int64_t)st->P.nx * st->P.ny : 0,
                          (int64_t)st->gst_host->steps);
+    hf::ctx_add_coop(st->ctx, (int64_t)st->gst_host->coop_cells);
     if (hf::ctx_timing_enabled(st->ctx)) {
         // ev0..ev1: CFL + dt + first flow; ev1..ev2: chemistry (order, kernel, commit,
         // validate); ev2..ev3: second flow
@@ -342,16 +345,18 @@ hf_status run_batch(hf_stepper* st, int nsteps, double cfl, cudaStream_t s, int*
     const bool failed = n > 0 && r.flags[n - 1] != 0;
     const int acc = failed ? n - 1 : n;
     double flux_ms = 0.0, chem_ms = 0.0;
-    int64_t attempts = 0;
+    int64_t attempts = 0, coop = 0;
     for (int i = 0; i < acc; ++i) {
         st->time += r.dt[i];
         attempts += (int64_t)r.steps[i];
+        coop += (int64_t)r.coop[i];
         flux_ms += 1e-6 * (double)((r.t[i][1] - r.t[i][0]) + (r.t[i][3] - r.t[i][2]));
         chem_ms += 1e-6 * (double)(r.t[i][2] - r.t[i][1]);
     }
     const int64_t nc = (int64_t)st->P.nx * st->P.ny;
     hf::ctx_add_launches(st->ctx, (st->run_kernels[0] + st->run_kernels[1]) / 2 * acc, st->chemistry ? nc * acc : 0,
                          attempts);
+    hf::ctx_add_coop(st->ctx, coop);
     if (hf::ctx_timing_enabled(st->ctx)) hf::ctx_add_timing(st->ctx, flux_ms, chem_ms, 0.0, 4 * acc, acc, 0);
     if (acc & 1) std::swap(st->buf[0], st->buf[3]);
     st->graph_steps += acc;
@@ -415,7 +420,7 @@ hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0
          cudaMalloc(&st->trial, sizeof(double) * st->nv * nc) == cudaSuccess &&
          cudaMalloc(&st->fail, sizeof(int) * nc) == cudaSuccess &&
          cudaMalloc(&st->order, sizeof(int32_t) * nc) == cudaSuccess &&
-         cudaMalloc(&st->bins, 16 * sizeof(unsigned long long)) == cudaSuccess;
+         cudaMalloc(&st->bins, hf::CHEM_BINS * sizeof(unsigned long long)) == cudaSuccess;
     for (int k = 0; ok && k < 4; ++k) ok = cudaEventCreate(&st->ev[k]) == cudaSuccess;
     if (ok) {
         std::vector<int64_t> idx(nc);

@@ -93,6 +93,8 @@ typedef struct hf_counters {
     int64_t chem_cell_calls;      /* chemistry_cell_calls */
     int64_t chem_steps;           /* accepted + rejected integrator steps */
     int64_t kernel_launches;      /* kernels launched by this context */
+    int64_t chem_coop_cells;      /* cells the batched chemistry integrated in groups of 8 lanes
+                                     (extension: the reference integrates one cell per thread) */
 } hf_counters;
 
 /* ---- context (replaces Cantera::newSolution(mechanism) + ChemistryBatch construction,
