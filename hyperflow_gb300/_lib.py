@@ -119,6 +119,8 @@ SIGNATURES = [
     ("hf_cfl_dt", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp, _d, _dp, _vp]),
     ("hf_validate", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(Patch), ctypes.c_int, _vp,
                            ctypes.POINTER(_i64), _vp]),
+    ("hf_set_chem_tuning", _i32, [_i32, _i32]),
+    ("hf_get_chem_tuning", None, [ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
     ("hf_repair_roundoff", _i32, [_vp, ctypes.c_int, ctypes.POINTER(Level), ctypes.POINTER(ctypes.POINTER(Patch)),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                   ctypes.POINTER(_i64), _vp]),

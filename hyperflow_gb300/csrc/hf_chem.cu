@@ -17,6 +17,7 @@
 // reaction structure, temperature exponents and activation temperatures are
 // compile-time constants of the generated mechanism table, so every species index
 // is a register index.
+#include <atomic>
 #include <cstdlib>
 #include "hf_chem_coop.cuh"
 
@@ -307,6 +308,33 @@ __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restr
     if (my_attempts) atomicAdd(&st->steps, my_attempts);
 }
 
+// Launch settings of the batched form, process-wide (hf_set_chem_tuning; the first use
+// reads HF_CHEM_MINB and HF_COOP_MIN_BUCKET / HF_COOP=0):
+//  * blocks of 64 lanes per SM the queue kernel's register budget is built for: 4 (255
+//    registers) or 5, 6, 8 (fewer registers, more resident lanes); the same per-cell code;
+//  * the cooperative queue takes cells that used at least 2^coop_min - 1 attempts in the
+//    previous call (coop_min = NBUCKET: no cooperative phase).
+std::atomic<int> g_tune_minb{0}, g_tune_coop{0};
+void chem_tuning(int* minb, int* coop_min) {
+    if (g_tune_minb.load() == 0) {
+        const char* e = getenv("HF_CHEM_MINB");
+        const int v = e ? atoi(e) : 4;
+        int expect = 0;
+        g_tune_minb.compare_exchange_strong(expect, (v == 5 || v == 6 || v == 8) ? v : 4);
+    }
+    if (g_tune_coop.load() == 0) {
+        const char* off = getenv("HF_COOP");
+        const char* e = getenv("HF_COOP_MIN_BUCKET");
+        int v = e ? atoi(e) : 5;
+        v = v < 1 ? 1 : (v > 16 ? 16 : v);
+        if (off && atoi(off) == 0) v = 16;
+        int expect = 0;
+        g_tune_coop.compare_exchange_strong(expect, v);
+    }
+    *minb = g_tune_minb.load();
+    *coop_min = g_tune_coop.load();
+}
+
 // Work-queue order: counting sort of cells by bucket = floor(log2(cost + 1)) (16
 // buckets), most expensive bucket first.  Cells of one bucket keep no particular
 // order; each cell's result does not depend on its position.
@@ -354,22 +382,8 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
                                      double* h_hist, int32_t* cost, int32_t* order, unsigned long long* bins,
                                      double* trial, int* fail, DevStatus* st, int sm_count, cudaStream_t s,
                                      int64_t* launches) {
-    // register budget of the queue kernel: 255 (4 blocks of 64 per SM) or 128 (8 blocks);
-    // HF_CHEM_MINB=8 selects the second.  Both run the same per-cell code.
-    static const int minb = [] {
-        const char* e = getenv("HF_CHEM_MINB");
-        const int v = e ? atoi(e) : 4;
-        return (v == 5 || v == 6 || v == 8) ? v : 4;
-    }();
-    // cooperative queue: cells that took at least 2^min_bucket - 1 attempts in the
-    // previous call (HF_COOP_MIN_BUCKET, default 5; HF_COOP=0 turns the phase off)
-    static const int coop_min = [] {
-        const char* off = getenv("HF_COOP");
-        if (off && atoi(off) == 0) return NBUCKET;
-        const char* e = getenv("HF_COOP_MIN_BUCKET");
-        const int v = e ? atoi(e) : 5;
-        return v < 1 ? 1 : (v > NBUCKET ? NBUCKET : v);
-    }();
+    int minb, coop_min;
+    chem_tuning(&minb, &coop_min);
     auto kern = minb == 8   ? k_chem_batched<NS, 8>
                 : minb == 6 ? k_chem_batched<NS, 6>
                 : minb == 5 ? k_chem_batched<NS, 5>
@@ -540,6 +554,23 @@ struct NoAllocScratch {
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 }  // namespace hf
+
+extern "C" hf_status hf_set_chem_tuning(int32_t blocks_per_sm, int32_t coop_min_bucket) {
+    if (blocks_per_sm < 0 || coop_min_bucket < 0 || coop_min_bucket > 16 ||
+        (blocks_per_sm && blocks_per_sm != 4 && blocks_per_sm != 5 && blocks_per_sm != 6 && blocks_per_sm != 8))
+        return HF_ERR_ARG;
+    int m = 0, c = 0;
+    hf::chem_tuning(&m, &c);  // settle the defaults first
+    if (blocks_per_sm) hf::g_tune_minb.store(blocks_per_sm);
+    if (coop_min_bucket) hf::g_tune_coop.store(coop_min_bucket);
+    return HF_OK;
+}
+extern "C" void hf_get_chem_tuning(int32_t* blocks_per_sm, int32_t* coop_min_bucket) {
+    int m = 0, c = 0;
+    hf::chem_tuning(&m, &c);
+    if (blocks_per_sm) *blocks_per_sm = m;
+    if (coop_min_bucket) *coop_min_bucket = c;
+}
 
 #include <mutex>
 

@@ -118,6 +118,16 @@ HF_EXPORT void hf_get_timing(const hf_ctx* ctx, double ms[3], int64_t launches[3
  * constant memory, one copy per device and process: the scale applies to every context
  * on the current device and to hf_chem_advance_noalloc until it is reset. */
 HF_EXPORT hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale);
+/* Launch settings of the batched chemistry form, process-wide (no counterpart in the
+ * reference; set by an autotuner, hyperflow_gb300/tune.py): blocks_per_sm, the resident
+ * 64-lane blocks per SM its register budget is built for (4, 5, 6 or 8; fewer registers
+ * per lane as it grows; the same per-cell code); coop_min_bucket b (1..16): cells that
+ * took at least 2^b - 1 step attempts in the previous call are integrated by groups of 8
+ * lanes (16: never).  0 leaves a setting unchanged.  Results are the same to rounding
+ * for any setting; with a fixed setting they are reproducible bit for bit.  The first
+ * use reads HF_CHEM_MINB and HF_COOP_MIN_BUCKET (HF_COOP=0: 16); defaults 4 and 5. */
+HF_EXPORT hf_status hf_set_chem_tuning(int32_t blocks_per_sm, int32_t coop_min_bucket);
+HF_EXPORT void hf_get_chem_tuning(int32_t* blocks_per_sm, int32_t* coop_min_bucket);
 
 /* Measured FP64 FMA throughput of the device (GFLOP/s, FMA = 2 flops): the FP64 roofline
  * denominator of the chemistry and flux kernels.  Independent FMA chains on every SM, best

@@ -1,0 +1,42 @@
+"""The autotuner (hyperflow_gb300/tune.py): a measured sweep of the batched chemistry's
+launch settings on a sample call, applied through hf_set_chem_tuning, and of the flux
+form on one Euler stage."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_chemistry_tuner_applies_the_fastest_candidate(gpu):
+    from hyperflow_gb300 import tune, workloads as W
+    U, _ = W.chem_batch(2048, seed=31, diluent="N2")
+    X = torch.from_numpy(U).cuda()
+    before = X.clone()
+    default = tune.get_chem_tuning(gpu)
+    try:
+        res = tune.tune_chemistry(gpu, X, 5e-7)
+        assert torch.equal(X, before)  # the sample call's input is not modified
+        sweep = res["sweep"]
+        assert len(sweep) == len(tune.CHEM_CANDIDATES) and all(r["ms"] > 0 for r in sweep)
+        best = min(sweep, key=lambda r: r["ms"])
+        assert res["best"] == (best["blocks_per_sm"], best["coop_min_bucket"]) == tune.get_chem_tuning(gpu)
+        # the cooperative phase runs for a low threshold and never for 16
+        assert any(r["coop_cells"] > 0 for r in sweep if r["coop_min_bucket"] <= 4)
+        assert all(r["coop_cells"] == 0 for r in sweep if r["coop_min_bucket"] == 16)
+    finally:
+        tune.set_chem_tuning(gpu, *default)
+    assert tune.get_chem_tuning(gpu) == default
+
+
+def test_flux_tuner_times_both_forms(gpu):
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import tune, workloads as W
+    U, lvd = W.det2d(seed=2, diluent="N2", nx=256, ny=64, hot_columns=16)
+    lv = hf.make_level(**lvd)
+    st = hf.Stepper(gpu, lv, torch.from_numpy(U).cuda(), flux="plain", chem="batched")
+    dt = st.cfl_dt(0.5)
+    res = tune.tune_flux(gpu, lv, st.state(), dt)
+    st.close()
+    assert set(res["ms"]) == {"plain", "fused"} and res["best"] in res["ms"]
+    assert all(np.isfinite(v) and v > 0 for v in res["ms"].values())
