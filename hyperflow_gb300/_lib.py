@@ -136,6 +136,8 @@ SIGNATURES = [
     ("hf_stepper_cfl_dt", _i32, [_vp, _d, _dp, _vp]),
     ("hf_stepper_stats", None, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     ("hf_stepper_set_graph", None, [_vp, ctypes.c_int]),
+    ("hf_stepper_graph_info", None, [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_i32),
+                                     ctypes.POINTER(ctypes.c_uint32)]),
 ]
 
 _lib = None

@@ -73,6 +73,10 @@ struct hf_stepper {
     double graph_cfl = -1.0;
     int use_graph = 1;
     int64_t graph_steps = 0, host_steps = 0;
+    unsigned last_graph_flags = 0;   // status flags of the last graph step (0: it was accepted)
+    unsigned* phase_flags = nullptr;  // device: the step's flags at its 4 phase boundaries
+    unsigned phase_flags_host[4] = {0, 0, 0, 0};
+    int capture_error = 0;           // cudaError_t of a failed capture (the graph path is then off)
     // device-resident runs
     RunRec* rec = nullptr;
     RunRec* rec_host = nullptr;
@@ -134,10 +138,18 @@ __global__ void k_run_record(hf::DevStatus* st, const double* ddt, RunRec* rec) 
     if (st->flags) st->abort_run = 1;
 }
 
-// Phase boundary k of a step: an event-record node (single steps) or a timestamp in
-// the run record (device-resident runs, whose graphs are launched many times).
+__global__ void k_phase_flags(const hf::DevStatus* st, unsigned* out, int k) { out[k] = st->flags; }
+
+// Phase boundary k of a step: an event-record node and the status flags so far (single
+// steps), or a timestamp in the run record (device-resident runs, whose graphs are
+// launched many times).
 cudaError_t phase_mark(hf_stepper* st, RunRec* rec, int k, cudaStream_t s, int64_t* nl) {
-    if (!rec) return cudaEventRecordWithFlags(st->ev[k], s, cudaEventRecordExternal);
+    if (!rec) {
+        k_phase_flags<<<1, 1, 0, s>>>(st->gst, st->phase_flags, k);
+        ++*nl;
+        const cudaError_t e = cudaGetLastError();
+        return e != cudaSuccess ? e : cudaEventRecordWithFlags(st->ev[k], s, cudaEventRecordExternal);
+    }
     k_run_mark<<<1, 1, 0, s>>>(st->gst, rec, k);
     ++*nl;
     return cudaGetLastError();
@@ -152,8 +164,10 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     const hf_patch& P = st->P;
     const int64_t nc = (int64_t)P.nx * P.ny;
     cudaError_t e;
-#define HF_Q(call) \
-    if ((e = (call)) != cudaSuccess) return e
+#define HF_Q(call)                                \
+    do {                                          \
+        if ((e = (call)) != cudaSuccess) return e; \
+    } while (0)
     HF_Q(cudaMemsetAsync(st->gst, 0, offsetof(DevStatus, abort_run), s));  // abort_run persists over a run
     HF_Q(cudaMemsetAsync(&st->gst->bad_cell, 0xff, sizeof(unsigned long long), s));
     HF_Q(phase_mark(st, rec, 0, s, nl));  // per-phase device time
@@ -177,13 +191,14 @@ cudaError_t enqueue_step(hf_stepper* st, double cfl, double* S0, double* T1, dou
     // commit, validate
     HF_Q(cudaMemsetAsync(&st->gst->counter, 0, 2 * sizeof(unsigned long long), s));  // work-queue heads
     if (st->chemistry) {
-        if (st->chem_form == HF_CHEM_PLAIN)  // the drop-in form: one thread per cell
+        if (st->chem_form == HF_CHEM_PLAIN) {  // the drop-in form: one thread per cell
             HF_Q(launch_chem(st->ns, HF_CHEM_PLAIN, X, P.comp_stride, st->cells, nc, 0.0, nullptr, st->rtol, st->atol,
                              st->trial, st->fail, st->gst, st->sm_count, s, nl, st->ddt));
-        else
+        } else {
             HF_Q(launch_chem_batched(st->ns, X, P.comp_stride, st->cells, nc, 0.0, st->ddt, nullptr, st->rtol,
                                      st->atol, st->hist.h, st->hist.cost, st->order, st->bins, st->trial, st->fail,
                                      st->gst, st->sm_count, s, nl));
+        }
         HF_Q(launch_chem_commit(st->ns, X, P.comp_stride, st->cells, nc, st->trial, s, nl));
         HF_Q(launch_validate(st->ns, P, X, 0, st->gst, s, nl));
     }
@@ -243,7 +258,9 @@ hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
     graphs_for_cfl(st, cfl);
     if (!st->exec[k]) {
         int64_t nl = 0;
-        if (capture_step(st, cfl, k, nullptr, &st->exec[k], &nl) != cudaSuccess) {
+        const cudaError_t ce = capture_step(st, cfl, k, nullptr, &st->exec[k], &nl);
+        if (ce != cudaSuccess) {
+            st->capture_error = (int)ce;
             st->use_graph = 0;  // host-controlled path from here on
             cudaGetLastError();
             return HF_ERR_CUDA;
@@ -253,6 +270,8 @@ hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
     if (cudaGraphLaunch(st->exec[k], s) != cudaSuccess ||
         cudaMemcpyAsync(st->gst_host, st->gst, sizeof(hf::DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaMemcpyAsync(st->ddt_host, st->ddt, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(st->phase_flags_host, st->phase_flags, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return HF_ERR_CUDA;
     hf::ctx_add_launches(st->ctx, st->graph_kernels[k], st->chemistry ? (int64_t)st->P.nx * st->P.ny : 0,
@@ -270,6 +289,7 @@ hf_status graph_step(hf_stepper* st, double cfl, double* dt, cudaStream_t s) {
             (void)cudaGetLastError();  // leave no pending error for the caller's next call
     }
     *dt = st->ddt_host[0];
+    st->last_graph_flags = st->gst_host->flags;
     return st->gst_host->flags ? HF_ERR_INADMISSIBLE : HF_OK;
 }
 
@@ -411,6 +431,8 @@ hf_status hf_stepper_create(hf_ctx* ctx, const hf_level* level, const double* U0
          cudaMemset(st->hist.h, 0, sizeof(double) * nc) == cudaSuccess &&
          cudaMemset(st->hist.cost, 0, sizeof(int32_t) * nc) == cudaSuccess &&
          cudaMalloc(&st->gst, sizeof(hf::DevStatus)) == cudaSuccess &&
+         cudaMalloc(&st->phase_flags, 4 * sizeof(unsigned)) == cudaSuccess &&
+         cudaMemset(st->phase_flags, 0, 4 * sizeof(unsigned)) == cudaSuccess &&
          cudaMemset(st->gst, 0, sizeof(hf::DevStatus)) == cudaSuccess &&
          cudaMalloc(&st->rec, sizeof(RunRec)) == cudaSuccess &&
          cudaMallocHost(&st->rec_host, sizeof(RunRec)) == cudaSuccess &&
@@ -464,6 +486,7 @@ void hf_stepper_destroy(hf_stepper* st) {
     cudaFree(st->cells);
     cudaFree(st->hist.h);
     cudaFree(st->hist.cost);
+    cudaFree(st->phase_flags);
     cudaFree(st->gst);
     cudaFreeHost(st->gst_host);
     cudaFree(st->rec);
@@ -478,6 +501,14 @@ void hf_stepper_destroy(hf_stepper* st) {
     cudaFree(st->fx);
     cudaFree(st->fy);
     delete st;
+}
+
+void hf_stepper_graph_info(const hf_stepper* st, uint32_t* last_flags, int32_t* capture_error,
+                           uint32_t* phase_flags) {
+    if (last_flags) *last_flags = st ? st->last_graph_flags : 0;
+    if (capture_error) *capture_error = st ? st->capture_error : 0;
+    if (phase_flags)
+        for (int k = 0; k < 4; ++k) phase_flags[k] = st ? st->phase_flags_host[k] : 0;
 }
 
 hf_status hf_stepper_step(hf_stepper* st, double cfl, double* dt, void* stream) {

@@ -568,6 +568,15 @@ class Stepper:
         self.ctx.lib.hf_stepper_stats(self.h, ctypes.byref(g), ctypes.byref(h))
         return {"graph_steps": g.value, "host_steps": h.value}
 
+    def graph_info(self):
+        """{"last_flags": status flags of the last graph step, "capture_error": CUDA error
+        of a failed capture (zeros: no fallback), "phase_flags": the last single graph
+        step's flags at its start, after the first flow, after the chemistry, after the
+        second flow}."""
+        f, e, ph = ctypes.c_uint32(0), ctypes.c_int32(0), (ctypes.c_uint32 * 4)()
+        self.ctx.lib.hf_stepper_graph_info(self.h, ctypes.byref(f), ctypes.byref(e), ph)
+        return {"last_flags": f.value, "capture_error": e.value, "phase_flags": list(ph)}
+
 
 # ------------------------------------------------------------------ block-AMR level operations
 class PatchSet:

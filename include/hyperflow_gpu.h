@@ -473,6 +473,14 @@ HF_EXPORT hf_status hf_stepper_cfl_dt(hf_stepper* st, double cfl, double* dt, vo
  * (every other case, and any graph step whose status reported a failure, re-run from the
  * untouched start state).  Extension: the reference has no device graph. */
 HF_EXPORT void hf_stepper_stats(const hf_stepper* st, int64_t* graph_steps, int64_t* host_steps);
+/* Why graph steps fall back to the host-controlled path: the status flags of the last
+ * graph step (0 when it was accepted; a failed cell or stage sets them), the CUDA error of
+ * a capture that failed (0 when none did; the graph path is then off), and (phase_flags,
+ * 4 entries, nullable) the last single graph step's flags at its start, after the CFL
+ * reduction and the first flow, after the chemistry and its validation, and after the
+ * second flow. */
+HF_EXPORT void hf_stepper_graph_info(const hf_stepper* st, uint32_t* last_flags, int32_t* capture_error,
+                                     uint32_t* phase_flags);
 /* Enable (default) or disable the graph path. */
 HF_EXPORT void hf_stepper_set_graph(hf_stepper* st, int enable);
 
