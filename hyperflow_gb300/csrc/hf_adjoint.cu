@@ -320,7 +320,7 @@ __device__ __noinline__ bool chem_vjp(double rho, double e, double& T, const dou
     if (!solve_T<NS>(z, e, Tn, m)) return false;
     T = Tn;
     KinCtx<NS> kc;
-    kin_setup<NS>(T, C, kc);
+    kin_setup<NS, false>(T, C, kc);
     double cpR[NS], dcpR[NS], cvk[NS], dTdy[N], cv, ETT;
     species_cp<NS>(T, cpR, dcpR);
     temp_grad<NS>(kc, cpR, y, dTdy, cvk, cv, ETT, nullptr);
@@ -416,7 +416,7 @@ __device__ __noinline__ bool chem_hess(double rho, double e, double& T, const do
     if (!solve_T<NS>(z, e, Tn, m)) return false;
     T = Tn;
     KinCtx<NS> kc;
-    kin_setup<NS>(T, C, kc);
+    kin_setup<NS, false>(T, C, kc);
     double cpR[NS], dcpR[NS], cvk[NS], dTdy[N], cv, ETT;
     species_cp<NS>(T, cpR, dcpR);
     temp_grad<NS>(kc, cpR, y, dTdy, cvk, cv, ETT, dcpR);
@@ -609,7 +609,7 @@ __device__ bool state_grads(const double* u, double* dT, double* dp, double& T) 
     comp<NS>(y, rho, z, C);
     if (!solve_T<NS>(z, e, T, m)) return false;
     KinCtx<NS> kc;
-    kin_setup<NS>(T, C, kc);
+    kin_setup<NS, false>(T, C, kc);
     double cpR[NS], dcpR[NS], cvk[NS], cv, ETT;
     species_cp<NS>(T, cpR, dcpR);
     temp_grad<NS>(kc, cpR, y, dT, cvk, cv, ETT, nullptr);

@@ -54,23 +54,6 @@ __device__ __forceinline__ void species_g_h(double T, double lnT, double invT, d
 }
 
 // ---------------------------------------------------------------- kinetics
-template <int R>
-__device__ __forceinline__ double arrhenius_T(double T, double lnT, double invT) {
-    constexpr double b = RXN[R].b, E = RXN[R].EaR;
-    if constexpr (b == 0.0 && E == 0.0) return 1.0;
-    else if constexpr (E == 0.0 && b == -1.0) return invT;
-    else if constexpr (E == 0.0 && b == -2.0) return invT * invT;
-    else if constexpr (b == 0.0) return exp(-E * invT);
-    else if constexpr (b == 2.0) return T * T * exp(-E * invT);
-    else return exp(fma(b, lnT, -E * invT));
-}
-template <int R>
-__device__ __forceinline__ double arrhenius0_T(double lnT, double invT) {
-    constexpr double b = RXN[R].b0, E = RXN[R].Ea0R;
-    if constexpr (b == 0.0 && E == 0.0) return 1.0;
-    else if constexpr (b == 0.0) return exp(-E * invT);
-    else return exp(fma(b, lnT, -E * invT));
-}
 template <int R, int NS>
 __device__ __forceinline__ double third_body(const double* C, double Csum) {
     constexpr Reaction rx = RXN[R];
@@ -135,6 +118,46 @@ __device__ __forceinline__ double troe_log10F(double T, double Pr, double* dPr, 
     return lFc * g;
 }
 
+// Temperature factors T^b exp(-E/T) of the rate constants, evaluated in one rolled
+// loop (one exp body for all reactions): k_inf of every reaction, then k_0 of the
+// falloff reactions in reaction order.  Kinds by (b, E): 1 (b = E = 0), 1/T and
+// 1/T^2 (E = 0, b = -1, -2), exp(-E/T) (b = 0), T*T*exp(-E/T) (b = 2), otherwise
+// exp(b lnT - E/T).
+enum : int { ARR_ONE = 0, ARR_INVT = 1, ARR_INVT2 = 2, ARR_EXP = 3, ARR_T2EXP = 4, ARR_EXPB = 5 };
+struct ArrTerm {
+    int kind;
+    double b, E;
+};
+constexpr int fall_index(int R) {
+    int n = 0;
+    for (int r = 0; r < R; ++r) n += RXN[r].type == RXN_FALLOFF ? 1 : 0;
+    return n;
+}
+constexpr int NFALL = fall_index(NR);
+struct ArrTable {
+    ArrTerm t[NR + NFALL];
+};
+constexpr ArrTable make_arr() {
+    ArrTable a{};
+    for (int r = 0; r < NR; ++r) {
+        const double b = RXN[r].b, E = RXN[r].EaR;
+        const int kind = (b == 0.0 && E == 0.0)   ? ARR_ONE
+                         : (E == 0.0 && b == -1.0) ? ARR_INVT
+                         : (E == 0.0 && b == -2.0) ? ARR_INVT2
+                         : (b == 0.0)              ? ARR_EXP
+                         : (b == 2.0)              ? ARR_T2EXP
+                                                   : ARR_EXPB;
+        a.t[r] = ArrTerm{kind, b, E};
+        if (RXN[r].type == RXN_FALLOFF) {
+            const double b0 = RXN[r].b0, E0 = RXN[r].Ea0R;
+            const int k0 = (b0 == 0.0 && E0 == 0.0) ? ARR_ONE : (b0 == 0.0) ? ARR_EXP : ARR_EXPB;
+            a.t[NR + fall_index(r)] = ArrTerm{k0, b0, E0};
+        }
+    }
+    return a;
+}
+__device__ constexpr ArrTable D_ARR = make_arr();
+
 // Per-evaluation shared quantities.
 template <int NS>
 struct KinCtx {
@@ -142,18 +165,40 @@ struct KinCtx {
     double eg[NS], ieg[NS];   // exp(g_k), exp(-g_k), g = g0/RT
     double hRT[NS];
     double rt_p0;             // R T / p0
+    double ar[NR + NFALL];    // temperature factors of k_inf (reactions) and k_0 (falloff)
 };
-template <int NS>
+// ARR: also the rate constants' temperature factors (the kinetics of the forward
+// chemistry; the adjoint evaluates its own).
+template <int NS, bool ARR = true>
 __device__ __forceinline__ void kin_setup(double T, const double* C, KinCtx<NS>& k) {
     k.T = T;
     k.lnT = log(T);
     k.invT = 1.0 / T;
     double g[NS];
     species_g_h<NS>(T, k.lnT, k.invT, g, k.hRT);
-#pragma unroll
+#pragma unroll 1
     for (int s = 0; s < NS; ++s) {
         k.eg[s] = exp(g[s]);
         k.ieg[s] = 1.0 / k.eg[s];
+    }
+    if constexpr (ARR) {
+#pragma unroll 1
+        for (int r = 0; r < NR + NFALL; ++r) {
+            const ArrTerm a = D_ARR.t[r];
+            double v;
+            if (a.kind == ARR_ONE) {
+                v = 1.0;
+            } else if (a.kind == ARR_INVT) {
+                v = k.invT;
+            } else if (a.kind == ARR_INVT2) {
+                v = k.invT * k.invT;
+            } else {
+                const double x = a.kind == ARR_EXPB ? fma(a.b, k.lnT, -a.E * k.invT) : -a.E * k.invT;
+                const double ex = exp(x);
+                v = a.kind == ARR_T2EXP ? k.T * k.T * ex : ex;
+            }
+            k.ar[r] = v;
+        }
     }
     double cs = 0.0;
 #pragma unroll
@@ -161,12 +206,20 @@ __device__ __forceinline__ void kin_setup(double T, const double* C, KinCtx<NS>&
     k.Csum = cs;
     k.rt_p0 = RU * T * (1.0 / ONE_ATM);
 }
+template <int R, int NS>
+__device__ __forceinline__ double kinf_T(const KinCtx<NS>& kc) {
+    return kc.ar[R];
+}
+template <int R, int NS>
+__device__ __forceinline__ double k0_T(const KinCtx<NS>& kc) {
+    return kc.ar[NR + fall_index(R)];
+}
 
 // Rate constant k (third-body factor included) of reaction R.
 template <int R, int NS>
 __device__ __forceinline__ double rate_k(const KinCtx<NS>& kc, const double* C, double& M) {
     constexpr Reaction rx = RXN[R];
-    const double kinf = c_A[R] * arrhenius_T<R>(kc.T, kc.lnT, kc.invT);
+    const double kinf = c_A[R] * kinf_T<R, NS>(kc);
     if constexpr (rx.type == RXN_ELEMENTARY) {
         M = 0.0;
         return kinf;
@@ -175,7 +228,7 @@ __device__ __forceinline__ double rate_k(const KinCtx<NS>& kc, const double* C, 
         return kinf * M;
     } else {
         M = third_body<R, NS>(C, kc.Csum);
-        const double k0 = c_A0[R] * arrhenius0_T<R>(kc.lnT, kc.invT);
+        const double k0 = c_A0[R] * k0_T<R, NS>(kc);
         const double Pr = k0 * M / kinf;
         const double lF = troe_log10F<R>(kc.T, Pr, nullptr, nullptr);
         return kinf * (Pr / (1.0 + Pr)) * exp10(lF);
@@ -226,7 +279,7 @@ __device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, d
                                         double* w = nullptr) {
     constexpr Reaction rx = RXN[R];
     constexpr int N = NS - 1;
-    const double kinf = c_A[R] * arrhenius_T<R>(kc.T, kc.lnT, kc.invT);
+    const double kinf = c_A[R] * kinf_T<R, NS>(kc);
     const double dlnkinf = rx.b * kc.invT + rx.EaR * kc.invT * kc.invT;
     double k, dkdT, dkdM = 0.0, M = 0.0;
     if constexpr (rx.type == RXN_ELEMENTARY) {
@@ -239,7 +292,7 @@ __device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, d
         dkdM = kinf;
     } else {
         M = third_body<R, NS>(C, kc.Csum);
-        const double k0 = c_A0[R] * arrhenius0_T<R>(kc.lnT, kc.invT);
+        const double k0 = c_A0[R] * k0_T<R, NS>(kc);
         const double dlnk0 = rx.b0 * kc.invT + rx.Ea0R * kc.invT * kc.invT;
         const double Pr = k0 * M / kinf;
         double dPr, dTF;
@@ -491,11 +544,10 @@ __device__ __forceinline__ double wrms(const double* v, const double* y0, const 
 // LU with partial pivoting in place (P A = L U); the diagonal holds 1/U_kk.
 template <int N>
 __device__ __forceinline__ bool lu_factor(double* A, int* piv) {
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
         int p = k;
         double best = fabs(A[k * N + k]);
-#pragma unroll
         for (int i = k + 1; i < N; ++i) {
             const double v = fabs(A[i * N + k]);
             if (v > best) { best = v; p = i; }
@@ -504,19 +556,13 @@ __device__ __forceinline__ bool lu_factor(double* A, int* piv) {
         piv[k] = p;
         if (p != k) {
 #pragma unroll
-            for (int i = k + 1; i < N; ++i)
-                if (i == p) {
-#pragma unroll
-                    for (int j = 0; j < N; ++j) { const double t = A[k * N + j]; A[k * N + j] = A[i * N + j]; A[i * N + j] = t; }
-                }
+            for (int j = 0; j < N; ++j) { const double t = A[k * N + j]; A[k * N + j] = A[p * N + j]; A[p * N + j] = t; }
         }
         const double inv = 1.0 / A[k * N + k];
         A[k * N + k] = inv;  // the solves multiply by the reciprocal pivot
-#pragma unroll
         for (int i = k + 1; i < N; ++i) {
             const double l = A[i * N + k] * inv;
             A[i * N + k] = l;
-#pragma unroll
             for (int j = k + 1; j < N; ++j) A[i * N + j] = fma(-l, A[k * N + j], A[i * N + j]);
         }
     }
@@ -524,22 +570,16 @@ __device__ __forceinline__ bool lu_factor(double* A, int* piv) {
 }
 template <int N>
 __device__ __forceinline__ void lu_solve(const double* A, const int* piv, double* b) {
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
         const int p = piv[k];
-        if (p != k) {
-#pragma unroll
-            for (int i = k + 1; i < N; ++i)
-                if (i == p) { const double t = b[k]; b[k] = b[i]; b[i] = t; }
-        }
+        if (p != k) { const double t = b[k]; b[k] = b[p]; b[p] = t; }
     }
-#pragma unroll
+#pragma unroll 1
     for (int i = 1; i < N; ++i)
-#pragma unroll
         for (int j = 0; j < i; ++j) b[i] = fma(-A[i * N + j], b[j], b[i]);
-#pragma unroll
+#pragma unroll 1
     for (int i = N - 1; i >= 0; --i) {
-#pragma unroll
         for (int j = i + 1; j < N; ++j) b[i] = fma(-A[i * N + j], b[j], b[i]);
         b[i] *= A[i * N + i];  // reciprocal pivot
     }
@@ -622,7 +662,7 @@ __device__ __noinline__ int cell_attempt(ChemCell<NS>& c, double rtol, double at
     for (int i = 0; i < N; ++i) Mx[i * N + i] += inv;
     bool ok = lu_factor<N>(Mx, piv);
     const double ih = 1.0 / c.h;
-#pragma unroll
+#pragma unroll 1
     for (int s = 0; s < 6; ++s) {
         if (!ok) break;
         const int base = s * (s - 1) / 2;
