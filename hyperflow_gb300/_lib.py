@@ -84,6 +84,7 @@ SIGNATURES = [
     ("hf_chem_advance", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, ctypes.c_int, ctypes.POINTER(_i64), _vp]),
     ("hf_chem_advance_batched", _i32, [_vp, _vp, _i64, _vp, _i64, _d, _vp, _d, _d, _vp, ctypes.POINTER(_i64), _vp]),
     ("hf_fp64_peak", _i32, [_vp, _dp, _vp]),
+    ("hf_fastmath_eval", _i32, [_vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     ("hf_amr_create", _i32, [_vp, ctypes.POINTER(Level), _vp, ctypes.POINTER(AmrOpts), ctypes.POINTER(_vp), _vp]),
     ("hf_amr_destroy", None, [_vp]),
     ("hf_amr_create_levels", _i32, [_vp, ctypes.POINTER(Level), ctypes.POINTER(_vp), ctypes.c_int,

@@ -555,6 +555,26 @@ static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 }  // namespace hf
 
+namespace hf {
+__global__ void k_fastmath(const double* __restrict__ x, int64_t n, double* __restrict__ e, double* __restrict__ ep,
+                           double* __restrict__ em, double* __restrict__ l) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    e[i] = fexp(v);
+    fexp_pair(v, ep[i], em[i]);
+    l[i] = flog(v);
+}
+}  // namespace hf
+extern "C" hf_status hf_fastmath_eval(const double* x, int64_t n, double* exp_out, double* pair_pos, double* pair_neg,
+                                      double* log_out, void* stream) {
+    if (n < 0 || !x || !exp_out || !pair_pos || !pair_neg || !log_out) return HF_ERR_ARG;
+    if (n == 0) return HF_OK;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    hf::k_fastmath<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(x, n, exp_out, pair_pos, pair_neg,
+                                                                              log_out);
+    return cudaGetLastError() == cudaSuccess ? HF_OK : HF_ERR_CUDA;
+}
 extern "C" hf_status hf_set_chem_tuning(int32_t blocks_per_sm, int32_t coop_min_bucket) {
     if (blocks_per_sm < 0 || coop_min_bucket < 0 || coop_min_bucket > 16 ||
         (blocks_per_sm && blocks_per_sm != 4 && blocks_per_sm != 5 && blocks_per_sm != 6 && blocks_per_sm != 8))

@@ -11,6 +11,7 @@
 #pragma once
 #include <utility>
 #include "hf_device.cuh"
+#include "hf_fastmath.cuh"
 #include "hf_internal.h"
 
 namespace hf {
@@ -87,11 +88,11 @@ __device__ __forceinline__ double troe_log10F(double T, double Pr, double* dPr, 
         Fcent = rx.troeA;
         dFcent = 0.0;
     } else {
-        const double e3 = exp(-T / rx.troeT3), e1 = exp(-T / rx.troeT1);
+        const double e3 = fexp(-T / rx.troeT3), e1 = fexp(-T / rx.troeT1);
         Fcent = (1 - rx.troeA) * e3 + rx.troeA * e1;
         dFcent = -(1 - rx.troeA) / rx.troeT3 * e3 - rx.troeA / rx.troeT1 * e1;
         if (rx.hasT2) {
-            const double e2 = exp(-rx.troeT2 / T);
+            const double e2 = fexp(-rx.troeT2 / T);
             Fcent += e2;
             dFcent += rx.troeT2 / (T * T) * e2;
         }
@@ -102,9 +103,9 @@ __device__ __forceinline__ double troe_log10F(double T, double Pr, double* dPr, 
         constexpr double c = const_log10(rx.troeA);  // F_cent is a constant of the table
         lFc = c;
     } else {
-        lFc = log10(fmax(Fcent, 1e-300));
+        lFc = flog(fmax(Fcent, 1e-300)) * fm::INV_LN10;
     }
-    const double lPr = log10(fmax(Pr, 1e-300));
+    const double lPr = flog(fmax(Pr, 1e-300)) * fm::INV_LN10;
     const double c = -0.4 - 0.67 * lFc, nn = 0.75 - 1.27 * lFc;
     const double x = lPr + c, den = nn - 0.14 * x;
     const double f1 = x / den;
@@ -172,14 +173,13 @@ struct KinCtx {
 template <int NS, bool ARR = true>
 __device__ __forceinline__ void kin_setup(double T, const double* C, KinCtx<NS>& k) {
     k.T = T;
-    k.lnT = log(T);
+    k.lnT = flog(T);
     k.invT = 1.0 / T;
     double g[NS];
     species_g_h<NS>(T, k.lnT, k.invT, g, k.hRT);
 #pragma unroll 1
     for (int s = 0; s < NS; ++s) {
-        k.eg[s] = exp(g[s]);
-        k.ieg[s] = 1.0 / k.eg[s];
+        fexp_pair(g[s], k.eg[s], k.ieg[s]);
     }
     if constexpr (ARR) {
 #pragma unroll 1
@@ -194,7 +194,7 @@ __device__ __forceinline__ void kin_setup(double T, const double* C, KinCtx<NS>&
                 v = k.invT * k.invT;
             } else {
                 const double x = a.kind == ARR_EXPB ? fma(a.b, k.lnT, -a.E * k.invT) : -a.E * k.invT;
-                const double ex = exp(x);
+                const double ex = fexp(x);
                 v = a.kind == ARR_T2EXP ? k.T * k.T * ex : ex;
             }
             k.ar[r] = v;
@@ -231,7 +231,7 @@ __device__ __forceinline__ double rate_k(const KinCtx<NS>& kc, const double* C, 
         const double k0 = c_A0[R] * k0_T<R, NS>(kc);
         const double Pr = k0 * M / kinf;
         const double lF = troe_log10F<R>(kc.T, Pr, nullptr, nullptr);
-        return kinf * (Pr / (1.0 + Pr)) * exp10(lF);
+        return kinf * (Pr / (1.0 + Pr)) * fexp(lF * fm::LN10);
     }
 }
 
@@ -297,7 +297,7 @@ __device__ __forceinline__ void add_jac(const KinCtx<NS>& kc, const double* C, d
         const double Pr = k0 * M / kinf;
         double dPr, dTF;
         const double lF = troe_log10F<R>(kc.T, Pr, &dPr, &dTF);
-        const double F = exp10(lF);
+        const double F = fexp(lF * fm::LN10);
         const double dlnk_dlnPr = 1.0 - Pr / (1.0 + Pr) + dPr;
         k = kinf * (Pr / (1.0 + Pr)) * F;
         dkdT = k * (dlnkinf + dlnk_dlnPr * (dlnk0 - dlnkinf) + dTF);
@@ -712,7 +712,7 @@ __device__ __noinline__ int cell_attempt(ChemCell<NS>& c, double rtol, double at
         if (!(c.h > 1e-300) || c.t + c.h == c.t) return CELL_FAIL;
         return CELL_CONTINUE;
     }
-    double hnew = c.h * fmin(6.0, fmax(0.2, 0.9 / pow(err, 0.25)));
+    double hnew = c.h * fmin(6.0, fmax(0.2, 0.9 / sqrt(sqrt(err))));
     if (err <= 1.0) {
         c.t = last ? c.tend : c.t + c.h;
 #pragma unroll

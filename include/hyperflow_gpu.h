@@ -134,6 +134,13 @@ HF_EXPORT void hf_get_chem_tuning(int32_t* blocks_per_sm, int32_t* coop_min_buck
  * of three timed launches after a warm-up.  Measurement utility; no reference counterpart. */
 HF_EXPORT hf_status hf_fp64_peak(hf_ctx* ctx, double* gflops, void* stream);
 
+/* The chemistry kernels' table-driven exponential and logarithm on n device values:
+ * exp_out = exp(x); pair_pos, pair_neg = exp(x), exp(-x) from the paired form;
+ * log_out = log(x).  Check utility (within a few ulp of the correctly rounded values);
+ * no reference counterpart. */
+HF_EXPORT hf_status hf_fastmath_eval(const double* x, int64_t n, double* exp_out, double* pair_pos, double* pair_neg,
+                                     double* log_out, void* stream);
+
 /* ---- EOS / flux primitives on batches (physics.cpp:4-48) ---- */
 /* properties(): q is SoA [NV][stride] device memory with count cells; writes p, a, T and
  * status[i] (0 ok, 1 inadmissible).  Returns HF_OK or HF_ERR_INADMISSIBLE if any failed. */
