@@ -250,8 +250,7 @@ __device__ __forceinline__ void gthermo(int t, double T, double lnT, double invT
     hRT = species_hRT(t, T, invT);
     const double sR =
         fma(a[0], lnT, fma(T, fma(T, fma(T, fma(T, a[4] * 0.25, a[3] * (1.0 / 3.0)), a[2] * 0.5), a[1]), a[6]));
-    eg = exp(hRT - sR);
-    ieg = 1.0 / eg;
+    fexp_pair(hRT - sR, eg, ieg);
 }
 
 // Third-body concentration of efficiency set q: sum_k eff_qk C_k.
@@ -268,7 +267,7 @@ __device__ __forceinline__ double gthird(const Grp& g, int q, double C, const do
 template <bool D>
 __device__ __forceinline__ double slot_k(const RxnSlot& s, double lnT, double invT, double M, double* dkdT,
                                          double* dkdM, double kA, double kA0) {
-    const double kinf = kA * exp(fma(s.b, lnT, -s.EaR * invT));
+    const double kinf = kA * fexp(fma(s.b, lnT, -s.EaR * invT));
     const double dlnkinf = s.b * invT + s.EaR * invT * invT;
     double k = kinf;
     if (s.type == RXN_THREE_BODY) {
@@ -278,15 +277,15 @@ __device__ __forceinline__ double slot_k(const RxnSlot& s, double lnT, double in
             *dkdM = kinf;
         }
     } else if (s.type == RXN_FALLOFF) {
-        const double k0 = kA0 * exp(fma(s.b0, lnT, -s.Ea0R * invT));
+        const double k0 = kA0 * fexp(fma(s.b0, lnT, -s.Ea0R * invT));
         const double Pr = k0 * M / kinf;
         const double lFc = s.lfc;
-        const double lPr = log10(fmax(Pr, 1e-300));
+        const double lPr = flog(fmax(Pr, 1e-300)) * fm::INV_LN10;
         const double c = -0.4 - 0.67 * lFc, nn = 0.75 - 1.27 * lFc;
         const double x = lPr + c, den = nn - 0.14 * x;
         const double f1 = x / den;
         const double gg = 1.0 / (1.0 + f1 * f1);
-        const double F = exp10(lFc * gg);
+        const double F = fexp(lFc * gg * fm::LN10);
         k = kinf * (Pr / (1.0 + Pr)) * F;
         if (D) {
             const double dPr = !(Pr > 1e-300) ? 0.0 : lFc * (-2.0 * f1 * gg * gg) * (nn / (den * den));
@@ -408,7 +407,7 @@ __device__ __noinline__ double grhs(double rho, double e, double yN2, double y, 
     double T = sh->T;
     __syncwarp(g.mask);
     if (!gsolve_T<NS>(g, z, zi, e, T, m)) return __longlong_as_double((long long)QNAN_BITS);
-    const double lnT = log(T), invT = 1.0 / T;
+    const double lnT = flog(T), invT = 1.0 / T;
     double eg, ieg, hRT;
     gthermo(g.t, T, lnT, invT, eg, ieg, hRT);
     grates<NS, false>(g, T, lnT, invT, C, Ci, eg, ieg, hRT, 0.0, sh);
@@ -434,7 +433,7 @@ __device__ __noinline__ double grhs_jac(double rho, double e, double yN2, double
     double T = sh->T;
     __syncwarp(g.mask);
     if (!gsolve_T<NS>(g, z, zi, e, T, m)) return __longlong_as_double((long long)QNAN_BITS);
-    const double lnT = log(T), invT = 1.0 / T;
+    const double lnT = flog(T), invT = 1.0 / T;
     double eg, ieg, hRT;
     gthermo(g.t, T, lnT, invT, eg, ieg, hRT);
     // dT/dy_j = -(e_j - e_L)/cv with e_k = R T / W_k (h_k/RT - 1), kept divided by rho
@@ -606,7 +605,7 @@ __device__ __forceinline__ int gattempt(const Grp& g, GInt& c, double& y, double
         if (!(c.h > 1e-300) || c.t + c.h == c.t) return CELL_FAIL;
         return CELL_CONTINUE;
     }
-    double hnew = c.h * fmin(6.0, fmax(0.2, 0.9 / pow(err, 0.25)));
+    double hnew = c.h * fmin(6.0, fmax(0.2, 0.9 / sqrt(sqrt(err))));
     if (err <= 1.0) {
         c.t = last ? c.tend : c.t + c.h;
         y = yn;
