@@ -204,6 +204,7 @@ hf_status hf_init(const char* mechanism, int device, hf_ctx** out) {
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->st_host, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->rep, repair_scratch_bytes());
     if (e == cudaSuccess) e = chem_set_rate_scale(nullptr);
+    if (e == cudaSuccess) e = chem_prefer_l1();
     if (e == cudaSuccess) e = adjoint_set_rate_scale(nullptr);
     if (e != cudaSuccess) {
         hf_destroy(ctx);

@@ -225,7 +225,7 @@ __device__ __forceinline__ void coop_phase(const double* __restrict__ U, int64_t
     if (my_attempts) atomicAdd(&st->steps, my_attempts);
 }
 
-template <int NS, int MINB>
+template <int NS, int MINB, bool COOP>
 __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restrict__ U, int64_t cs,
                                                      const int64_t* __restrict__ cell_index,
                                                      const int32_t* __restrict__ order, int64_t count, double dt,
@@ -237,12 +237,16 @@ __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restr
     if (st->abort_run) return;  // an earlier step of this device-resident run failed
     const unsigned lane = threadIdx.x & 31;
     if (dt_dev) dt = *dt_dev;  // interval from device memory (graph-captured steps)
-    // the costliest cells first, one cell per group of 8 lanes; the rest one per lane
-    const int64_t ncoop = (order && coop_n) ? (int64_t)*coop_n : 0;
-    if (ncoop > 0) {
-        __shared__ coop::GShared sh[2][4];  // 64-thread blocks: 2 warps of 4 groups
-        coop_phase<NS>(U, cs, cell_index, order, count, ncoop, dt, dt_cell, rtol, atol, trial, fail, h_hist, cost,
-                       st, &sh[threadIdx.x >> 5][(threadIdx.x & 31) >> 3]);
+    // COOP: the costliest cells first, one cell per group of 8 lanes; the rest one per
+    // lane.  Without it the kernel holds no shared memory (the L1 keeps the lanes' stacks).
+    int64_t ncoop = 0;
+    if constexpr (COOP) {
+        ncoop = (order && coop_n) ? (int64_t)*coop_n : 0;
+        if (ncoop > 0) {
+            __shared__ coop::GShared sh[2][4];  // 64-thread blocks: 2 warps of 4 groups
+            coop_phase<NS>(U, cs, cell_index, order, count, ncoop, dt, dt_cell, rtol, atol, trial, fail, h_hist,
+                           cost, st, &sh[threadIdx.x >> 5][(threadIdx.x & 31) >> 3]);
+        }
     }
     ChemCell<NS> c;
     int64_t cell = -1;
@@ -313,7 +317,8 @@ __global__ void __launch_bounds__(64, MINB) k_chem_batched(const double* __restr
 //  * blocks of 64 lanes per SM the queue kernel's register budget is built for: 4 (255
 //    registers) or 5, 6, 8 (fewer registers, more resident lanes); the same per-cell code;
 //  * the cooperative queue takes cells that used at least 2^coop_min - 1 attempts in the
-//    previous call (coop_min = NBUCKET: no cooperative phase).
+//    previous call (coop_min = NBUCKET, the default: no cooperative phase, and the kernel
+//    instance without it).
 std::atomic<int> g_tune_minb{0}, g_tune_coop{0};
 void chem_tuning(int* minb, int* coop_min) {
     if (g_tune_minb.load() == 0) {
@@ -325,7 +330,7 @@ void chem_tuning(int* minb, int* coop_min) {
     if (g_tune_coop.load() == 0) {
         const char* off = getenv("HF_COOP");
         const char* e = getenv("HF_COOP_MIN_BUCKET");
-        int v = e ? atoi(e) : 5;
+        int v = e ? atoi(e) : 16;
         v = v < 1 ? 1 : (v > 16 ? 16 : v);
         if (off && atoi(off) == 0) v = 16;
         int expect = 0;
@@ -384,10 +389,15 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
                                      int64_t* launches) {
     int minb, coop_min;
     chem_tuning(&minb, &coop_min);
-    auto kern = minb == 8   ? k_chem_batched<NS, 8>
-                : minb == 6 ? k_chem_batched<NS, 6>
-                : minb == 5 ? k_chem_batched<NS, 5>
-                            : k_chem_batched<NS, 4>;
+    const bool coop = coop_min < NBUCKET;
+    auto kern = coop ? (minb == 8   ? k_chem_batched<NS, 8, true>
+                        : minb == 6 ? k_chem_batched<NS, 6, true>
+                        : minb == 5 ? k_chem_batched<NS, 5, true>
+                                    : k_chem_batched<NS, 4, true>)
+                     : (minb == 8   ? k_chem_batched<NS, 8, false>
+                        : minb == 6 ? k_chem_batched<NS, 6, false>
+                        : minb == 5 ? k_chem_batched<NS, 5, false>
+                                    : k_chem_batched<NS, 4, false>);
     const int bs = 64;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
@@ -414,6 +424,20 @@ static cudaError_t chem_batched_impl(double* U, int64_t cs, const int64_t* idx, 
                                          cost, coop_n, st);
     ++*launches;
     return cudaGetLastError();
+}
+// The batched kernel instances without the cooperative phase use no shared memory: the
+// unified L1 / shared storage goes to L1, which caches the lanes' stack frames.
+cudaError_t chem_prefer_l1() {
+    const void* kernels[] = {(const void*)k_chem_batched<9, 4, false>,  (const void*)k_chem_batched<9, 5, false>,
+                             (const void*)k_chem_batched<9, 6, false>,  (const void*)k_chem_batched<9, 8, false>,
+                             (const void*)k_chem_batched<10, 4, false>, (const void*)k_chem_batched<10, 5, false>,
+                             (const void*)k_chem_batched<10, 6, false>, (const void*)k_chem_batched<10, 8, false>};
+    for (const void* k : kernels) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                   (int)cudaSharedmemCarveoutMaxL1);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 cudaError_t launch_chem_batched(int ns, double* U, int64_t cs, const int64_t* idx, int64_t count, double dt,
                                 const double* dt_dev, const double* dtc, double rtol, double atol, double* h_hist,

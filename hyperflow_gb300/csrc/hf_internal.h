@@ -119,6 +119,8 @@ cudaError_t launch_interp(int ns, const hf_patch& C, const double* Uc, const hf_
 
 // Chemistry (hf_chem.cu)
 cudaError_t chem_set_rate_scale(const double* scale);
+// L1 preference of the batched chemistry kernels without shared memory (once per context)
+cudaError_t chem_prefer_l1();
 
 // Discrete adjoint of 0D chemistry runs (hf_adjoint.cu).  Scratch arrays are
 // [slot][component][chunk] with chunk the stride.

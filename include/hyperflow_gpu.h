@@ -125,7 +125,7 @@ HF_EXPORT hf_status hf_set_rate_scale(hf_ctx* ctx, const double* scale);
  * took at least 2^b - 1 step attempts in the previous call are integrated by groups of 8
  * lanes (16: never).  0 leaves a setting unchanged.  Results are the same to rounding
  * for any setting; with a fixed setting they are reproducible bit for bit.  The first
- * use reads HF_CHEM_MINB and HF_COOP_MIN_BUCKET (HF_COOP=0: 16); defaults 4 and 5. */
+ * use reads HF_CHEM_MINB and HF_COOP_MIN_BUCKET (HF_COOP=0: 16); defaults 4 and 16. */
 HF_EXPORT hf_status hf_set_chem_tuning(int32_t blocks_per_sm, int32_t coop_min_bucket);
 HF_EXPORT void hf_get_chem_tuning(int32_t* blocks_per_sm, int32_t* coop_min_bucket);
 

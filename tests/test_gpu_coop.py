@@ -1,5 +1,6 @@
-"""The batched chemistry's cooperative phase (hyperflow_gb300/csrc/hf_chem_coop.cuh): cells
-whose previous call took at least 31 step attempts are integrated by groups of 8 lanes,
+"""The batched chemistry's cooperative phase (hyperflow_gb300/csrc/hf_chem_coop.cuh), set
+on here (hf_set_chem_tuning): cells whose previous call took at least 31 step attempts
+are integrated by groups of 8 lanes,
 the rest one per lane.  Results stay within the chemistry parity bar against the oracle
 (T relative 1e-6, Y absolute 1e-8 of the cell's density), with the file's 9 species and
 with the inert AR extension, in a chemistry batch and inside the stepper's graph steps."""
@@ -8,6 +9,16 @@ import pytest
 import torch
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def cooperative(gpu):
+    """The cooperative phase for cells of at least 31 attempts (off by default)."""
+    from hyperflow_gb300 import tune
+    before = tune.get_chem_tuning(gpu)
+    tune.set_chem_tuning(gpu, 0, 5)
+    yield
+    tune.set_chem_tuning(gpu, *before)
 
 
 def cuda(a):

@@ -1,6 +1,6 @@
 """The autotuner (hyperflow_gb300/tune.py): a measured sweep of the batched chemistry's
-launch settings on a sample call, applied through hf_set_chem_tuning, and of the flux
-form on one Euler stage."""
+launch settings on a sample call, applied through hf_set_chem_tuning when it beats the
+default by the tuner's margin, and of the flux form on one Euler stage."""
 import numpy as np
 import pytest
 import torch
@@ -20,6 +20,9 @@ def test_chemistry_tuner_applies_the_fastest_candidate(gpu):
         sweep = res["sweep"]
         assert len(sweep) == len(tune.CHEM_CANDIDATES) and all(r["ms"] > 0 for r in sweep)
         best = min(sweep, key=lambda r: r["ms"])
+        base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == tune.CHEM_DEFAULT][0]
+        if best["ms"] > (1.0 - tune.MARGIN) * base["ms"]:
+            best = base  # the default stays unless a candidate beats it by the margin
         assert res["best"] == (best["blocks_per_sm"], best["coop_min_bucket"]) == tune.get_chem_tuning(gpu)
         # the cooperative phase runs for a low threshold and never for 16
         assert any(r["coop_cells"] > 0 for r in sweep if r["coop_min_bucket"] <= 4)
