@@ -382,6 +382,12 @@ def run_ours(args):
         del Xt, Ut
         if args.flux == "auto":
             flux = tuning["flux"]["best"]
+        # the cooperative threshold over whole graph steps at the chosen register budget
+        m = tuning["chemistry"]["best"][0]
+        tuning["stepper"] = tune.tune_stepper(ctx, level, torch.from_numpy(U0).cuda(), args.cfl, flux=flux,
+                                              warm=args.warmup, steps=4,
+                                              candidates=[(m, 16), (m, 3), (m, 5), (m, 7)])
+        tuning["stepper"]["sample"] = "4 graph steps after %d warm-up steps per candidate" % args.warmup
     args.flux = flux
 
     if args.probe_only:
@@ -608,6 +614,15 @@ def run_ours(args):
         # 3000 K, Ar diluent): device-resident graph steps of the headline forms from t = 0;
         # few stiff cells, so single cells' chemistry sets the step time
         U1, l1 = W.det1d(diluent="AR", nx=2000)
+        tuning1 = None
+        if not args.no_tune:
+            # a few thousand cells: the stiff cells' serial chains set the step, and the
+            # cooperative phase pays here (tuned on this workload, then restored)
+            from hyperflow_gb300 import tune
+            restore = tune.get_chem_tuning(ctx)
+            tuning1 = tune.tune_stepper(ctx, hf.make_level(**l1), torch.from_numpy(U1).cuda(), args.cfl,
+                                        flux=args.flux, warm=20, steps=20)
+            tuning1["sample"] = "20 graph steps after 20 from t = 0 per candidate"
         s1 = hf.Stepper(ctx, hf.make_level(**l1), torch.from_numpy(U1).cuda(), flux=args.flux, chem="batched")
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -620,8 +635,10 @@ def run_ours(args):
                              "reflecting left/top/bottom, transmissive right, CFL %.2f; %d device-resident steps "
                              "from t = 0" % (args.cfl, done1),
                  "value": 4000 * done1 / (ms1 * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms1 / max(done1, 1),
-                 "final_time": s1.time}
+                 "final_time": s1.time, "tuning": tuning1}
         s1.close()
+        if tuning1 is not None:
+            tune.set_chem_tuning(ctx, *restore)
         if not args.no_cpu and args.det1d_cpu_steps > 0:
             oracle = _oracle(10)
             g1 = oracle.make_grid(2000, 2, l1["dx"], l1["dy"], periodic=(0, 0), bc_lo=(0, 0), bc_hi=(1, 0),

@@ -11,6 +11,12 @@
   MARGIN faster on the sample: one call stands for the steps that follow, and a
   cooperative setting whose queue stays empty on the sample can still engage, and cost,
   in later steps.
+* Stepper chemistry (tune_stepper): the same settings timed over a few whole graph
+  steps of the caller's stepper from one start state, each candidate from a fresh
+  stepper (its history builds up over the steps as it does in a run, so a cooperative
+  setting shows whether its queue engages and pays).  Small, tail-bound problems (a 1D
+  detonation of a few thousand cells) gain from the cooperative phase; large ones lose
+  throughput to it.
 * Flux form: one Euler stage of the workload's state with the plain per-face kernels and
   with the fused TMA-tile kernel (32 x 7 cells per CTA), each timed after a warm-up; the
   faster form is returned for the caller's stepper.
@@ -28,6 +34,7 @@ from . import solver as S
 CHEM_DEFAULT = (4, 16)
 CHEM_CANDIDATES = [CHEM_DEFAULT, (5, 16), (6, 16), (8, 16), (4, 3), (4, 5), (4, 7)]
 MARGIN = 0.03
+STEP_CANDIDATES = [CHEM_DEFAULT, (4, 3), (4, 5), (4, 7)]
 
 
 def get_chem_tuning(ctx):
@@ -100,3 +107,40 @@ def tune_flux(ctx, level, U, dt, repeats=3):
         torch.cuda.synchronize()
         ms[name] = e0.elapsed_time(e1) / repeats
     return {"best": min(ms, key=ms.get), "ms": ms}
+
+
+def tune_stepper(ctx, level, U, cfl, flux="plain", warm=2, steps=6, candidates=STEP_CANDIDATES, apply=True):
+    """U: (NV, ny, nx) state; the batched chemistry settings timed over `steps` graph steps
+    (after `warm` steps) of a fresh stepper per candidate.  Returns {"best": (...),
+    "sweep": [{"blocks_per_sm", "coop_min_bucket", "ms_per_step", "coop_cells"}]} and, with
+    apply, leaves the best setting in force (the default unless one beats it by MARGIN)."""
+    before = get_chem_tuning(ctx)
+    sweep = []
+    try:
+        for minb, coop in candidates:
+            set_chem_tuning(ctx, minb, coop)
+            st = S.Stepper(ctx, level, U, flux=flux, chem="batched")
+            try:
+                for _ in range(warm):
+                    st.step(cfl=cfl)
+                c0 = ctx.counters()
+                torch.cuda.synchronize()
+                e0, e1 = _events()
+                e0.record()
+                st.run(steps, cfl=cfl)
+                e1.record()
+                torch.cuda.synchronize()
+                c1 = ctx.counters()
+            finally:
+                st.close()
+            sweep.append({"blocks_per_sm": minb, "coop_min_bucket": coop, "ms_per_step": e0.elapsed_time(e1) / steps,
+                          "coop_cells": c1["chem_coop_cells"] - c0["chem_coop_cells"]})
+    finally:
+        set_chem_tuning(ctx, *before)
+    best = min(sweep, key=lambda r: r["ms_per_step"])
+    base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == CHEM_DEFAULT]
+    if base and best["ms_per_step"] > (1.0 - MARGIN) * base[0]["ms_per_step"]:
+        best = base[0]
+    if apply:
+        set_chem_tuning(ctx, best["blocks_per_sm"], best["coop_min_bucket"])
+    return {"best": (best["blocks_per_sm"], best["coop_min_bucket"]), "sweep": sweep}

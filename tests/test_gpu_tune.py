@@ -43,3 +43,26 @@ def test_flux_tuner_times_both_forms(gpu):
     st.close()
     assert set(res["ms"]) == {"plain", "fused"} and res["best"] in res["ms"]
     assert all(np.isfinite(v) and v > 0 for v in res["ms"].values())
+
+
+def test_stepper_tuner_times_whole_steps(gpu):
+    """tune_stepper: each candidate from a fresh stepper over whole graph steps; the
+    default (no cooperative phase) stays unless a candidate beats it by the margin, and the
+    cooperative candidate's queue engages on the stiff 1D detonation."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import tune, workloads as W
+    U, lvd = W.det1d(diluent="AR", nx=400)
+    lv = hf.make_level(**lvd)
+    default = tune.get_chem_tuning(gpu)
+    try:
+        res = tune.tune_stepper(gpu, lv, torch.from_numpy(U).cuda(), 0.5, warm=10, steps=10,
+                                candidates=[tune.CHEM_DEFAULT, (4, 3)])
+        sweep = res["sweep"]
+        assert [(r["blocks_per_sm"], r["coop_min_bucket"]) for r in sweep] == [tune.CHEM_DEFAULT, (4, 3)]
+        assert all(r["ms_per_step"] > 0 for r in sweep)
+        assert sweep[0]["coop_cells"] == 0 and sweep[1]["coop_cells"] > 0
+        base, other = sweep
+        want = (4, 3) if other["ms_per_step"] <= (1 - tune.MARGIN) * base["ms_per_step"] else tune.CHEM_DEFAULT
+        assert res["best"] == want == tune.get_chem_tuning(gpu)
+    finally:
+        tune.set_chem_tuning(gpu, *default)
