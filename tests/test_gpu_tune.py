@@ -51,7 +51,7 @@ def test_stepper_tuner_times_whole_steps(gpu):
     cooperative candidate's queue engages on the stiff 1D detonation."""
     import hyperflow_gb300 as hf
     from hyperflow_gb300 import tune, workloads as W
-    U, lvd = W.det1d(diluent="AR", nx=400)
+    U, lvd = W.det1d(diluent="N2", nx=400)
     lv = hf.make_level(**lvd)
     default = tune.get_chem_tuning(gpu)
     try:
