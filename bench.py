@@ -35,13 +35,16 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-steps/s, 2D H2 detonation FP64: batched vs plain GPU; adjoint/forward time"
 NX, NY = 2048, 512
 STRIP_ROWS = 32  # rows of the periodic strip the CPU legs time
-# FP64 thread instructions of k_chem_batched per integrator step attempt (DFMA x 2 + DADD
-# + DMUL, from ncu's instruction counts of one launch of the 512 x 128 detonation over
-# the launch's attempts): the executed-flop figure beside the algorithmic one.
-EXECUTED_FLOPS_PER_ATTEMPT = 1.79e4
-# DRAM bytes that ncu measured for one full-size k_chem_batched launch of the probe below
-# (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
-PROBE_TRAFFIC = None
+# From one ncu capture of the probe launch below at the full size (2048 x 512, the state
+# after the 3 warm-up and 8 timed steps; `bench.py --probe-only --warmup 11`, the second
+# k_chem_batched launch of the probe, 1,090,021 step attempts, k_chem_batched<10, 4, 0>):
+# * FP64 flops per integrator step attempt (DFMA x 2 + DADD + DMUL thread instructions
+#   over the launch's attempts; the screened cells' kinetics pass is included), the
+#   executed-flop figure beside the algorithmic one;
+# * DRAM bytes of that launch (dram__bytes_read.sum + dram__bytes_write.sum): mostly the
+#   lanes' stack frames written back from L2.
+EXECUTED_FLOPS_PER_ATTEMPT = 2.063e4
+PROBE_TRAFFIC = 5011249000
 # algorithmic HBM bytes of one cell-step (NS = 10): 4 Euler stages reading U (and U_old in
 # the Heun stages) and writing U, plus chemistry reading and writing U
 BYTES_PER_CELL_STEP = 1248
@@ -705,7 +708,8 @@ def run_ours(args):
             "peak_source": "measured in this run (hf_fp64_peak: independent DFMA chains on every SM)",
             "executed": {"achieved": EXECUTED_FLOPS_PER_ATTEMPT * probe["gpu_attempts"] / (launch_ms * 1e-3) / 1e9,
                          "flops_per_attempt": EXECUTED_FLOPS_PER_ATTEMPT,
-                         "note": "ncu FP64 instruction count per integrator step attempt x the launch's attempts"}}
+                         "note": "ncu FP64 instruction count per integrator step attempt (this probe launch, "
+                                 "profiles/k_chem_batched_2048x512_probe.md) x the launch's attempts"}}
     if "algorithmic" in probe:
         alg = probe["algorithmic"]
         fp64["achieved"] = alg["flops"] / (launch_ms * 1e-3) / 1e9
@@ -714,6 +718,8 @@ def run_ours(args):
         fp64["algorithmic_flops_per_launch"] = alg["flops"]
     roof = {"kernel": "k_chem_batched", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": PROBE_TRAFFIC,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this probe launch at full size "
+                              "(profiles/k_chem_batched_2048x512_probe.md)",
             "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
             "fp64": fp64,
