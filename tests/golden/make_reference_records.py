@@ -2,7 +2,8 @@
 checks (HyperFlow_V3/docs/case_checks.json and docs/amr_checks.json), reduced to the
 fields the oracle and GPU tests compare with; and reference_cases.json: the keys of its
 two smoke case configurations (cases/*/smoke.json) that the case loader reads.  Run
-where the reference tree is present:
+where the reference tree is present, with its HyperFlow_V3 directory as the one required
+argument:
 
     python tests/golden/make_reference_records.py /root/reference/HyperFlow_V3
 """
@@ -58,4 +59,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/HyperFlow_V3")
+    if len(sys.argv) != 2 or not os.path.isdir(os.path.join(sys.argv[1], "docs")):
+        sys.exit("usage: python tests/golden/make_reference_records.py <HyperFlow_V3 directory of the reference tree>")
+    main(sys.argv[1])
