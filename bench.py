@@ -708,8 +708,8 @@ def run_ours(args):
             "peak_source": "measured in this run (hf_fp64_peak: independent DFMA chains on every SM)",
             "executed": {"achieved": EXECUTED_FLOPS_PER_ATTEMPT * probe["gpu_attempts"] / (launch_ms * 1e-3) / 1e9,
                          "flops_per_attempt": EXECUTED_FLOPS_PER_ATTEMPT,
-                         "note": "ncu FP64 instruction count per integrator step attempt (this probe launch, "
-                                 "profiles/k_chem_batched_2048x512_probe.md) x the launch's attempts"}}
+                         "note": "ncu FP64 instruction count per integrator step attempt (one capture of this "
+                                 "probe launch at full size) x the launch's attempts"}}
     if "algorithmic" in probe:
         alg = probe["algorithmic"]
         fp64["achieved"] = alg["flops"] / (launch_ms * 1e-3) / 1e9
@@ -718,8 +718,8 @@ def run_ours(args):
         fp64["algorithmic_flops_per_launch"] = alg["flops"]
     roof = {"kernel": "k_chem_batched", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": PROBE_TRAFFIC,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this probe launch at full size "
-                              "(profiles/k_chem_batched_2048x512_probe.md)",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one capture of this probe "
+                              "launch at full size (bench.py --probe-only --warmup 11, its second k_chem_batched launch)",
             "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
             "fp64": fp64,

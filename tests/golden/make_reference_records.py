@@ -5,7 +5,7 @@ two smoke case configurations (cases/*/smoke.json) that the case loader reads.  
 where the reference tree is present, with its HyperFlow_V3 directory as the one required
 argument:
 
-    python tests/golden/make_reference_records.py /root/reference/HyperFlow_V3
+    python tests/golden/make_reference_records.py <reference tree>/HyperFlow_V3
 """
 import json
 import os
