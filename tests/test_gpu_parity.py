@@ -361,6 +361,29 @@ def test_graph_step_equals_host_step(gpu, flux, chem):
     assert a.time == b.time
 
 
+def test_graph_step_phase_flags(gpu):
+    """hf_stepper_graph_info: an accepted graph step has no flag at any of its four phase
+    boundaries; a graph step at 8 times the CFL number fails on the device (and is re-run
+    with host control), and its flags only accumulate from phase to phase up to the
+    step's final flags."""
+    import hyperflow_gb300 as hf
+    from hyperflow_gb300 import workloads as W
+    U, lvd = W.det2d(seed=2, diluent="N2", nx=96, ny=24, hot_columns=8)
+    lv = hf.make_level(**lvd)
+    s = hf.Stepper(gpu, lv, cuda(U), flux="plain", chem="batched")
+    s.step(cfl=0.5)
+    info = s.graph_info()
+    assert s.stats()["graph_steps"] == 1
+    assert info == {"last_flags": 0, "capture_error": 0, "phase_flags": [0, 0, 0, 0]}
+    s.step(cfl=8.0)
+    info = s.graph_info()
+    assert s.stats()["host_steps"] == 1 and info["capture_error"] == 0
+    ph = info["phase_flags"]
+    assert info["last_flags"] != 0 and ph[3] == info["last_flags"]
+    assert all((ph[k] & ph[k + 1]) == ph[k] for k in range(3))
+    s.close()
+
+
 @pytest.mark.parametrize("flux,cfl,chem", [("fused", 0.5, "batched"), ("fused", 8.0, "batched"),
                                           ("plain", 0.5, "batched"), ("plain", 8.0, "batched"),
                                           ("plain", 0.5, "plain"), ("plain", 8.0, "plain")])
