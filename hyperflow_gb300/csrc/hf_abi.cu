@@ -64,9 +64,7 @@ cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 cudaError_t reset_status(hf_ctx* ctx, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(ctx->st, 0, sizeof(DevStatus), s);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(&ctx->st->bad_cell, 0xff, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
-    return cudaMemsetAsync(&ctx->st->donor[0], 0xff, sizeof(ctx->st->donor), s);
+    return cudaMemsetAsync(&ctx->st->bad_cell, 0xff, sizeof(unsigned long long), s);
 }
 // Timing brackets: tic() before a class's launches, toc() after them; the elapsed
 // time is collected at the next stream synchronisation (read_status).

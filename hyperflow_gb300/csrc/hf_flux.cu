@@ -1,13 +1,14 @@
 // Flux path kernels: ghost fill, Euler-stage flux + update (plain and fused
-// forms), Heun combine, validation, roundoff repair, CFL reduction, and the
-// coarse->fine conservative interpolation.  Reference semantics:
+// forms), Heun combine, validation, CFL reduction, and the coarse->fine
+// conservative interpolation (the roundoff repair is in hf_amr.cu).  Reference
+// semantics:
 //   ghost fill      HyperFlow_V3/src/BlockAMR.cpp:48-59,137-146; src/FlowBoundary.hpp:12-36
 //                   (AMReX FillPatchSingleLevel: FillBoundary, then filcc per cell and the
 //                   FlowBoundary functor, faces before corners)
 //   Euler stage     BlockAMR.cpp:210-243 (MUSCL on conserved variables, admissibility
 //                   fallback per face side, HLLC, wall-flux override, flux divergence)
 //   Heun combine    BlockAMR.cpp:266-269
-//   validate        BlockAMR.cpp:286-298;  repairRoundoff BlockAMR.cpp:299-334
+//   validate        BlockAMR.cpp:286-298
 //   stableDt        BlockAMR.cpp:335-346
 //   interpolation   src/ConservativeInterp.cpp:18-51
 #include <cuda.h>
@@ -769,91 +770,6 @@ cudaError_t launch_cfl(int ns, const Level& L, const hf_patch& P, const double* 
                        int64_t* launches) {
     const int64_t n = (int64_t)P.nx * P.ny;
     HF_DISPATCH(ns, k_cfl)<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(L, P, U, st);
-    ++*launches;
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------- roundoff repair
-// pass 0: per-species peak (max partial density; non-negative doubles order like
-// their bit patterns).  pass 1: donor = lowest linear index holding the peak
-// (BlockAMR.cpp:310 keeps the first cell with the largest mass, all volumes equal
-// on one level).  pass 2: zero roundoff negatives, accumulate deficits, flag
-// materially negative values (BlockAMR.cpp:319-324).
-template <int NS>
-__global__ void k_repair_scan(hf_patch P, const double* __restrict__ U, int64_t cell_base, int pass, DevStatus* st) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)P.nx * P.ny) return;
-    const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
-    const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
-    for (int n = 0; n < NS; ++n) {
-        const double v = U[g + n * P.comp_stride];
-        if (pass == 0) {
-            if (v > 0.0) atomicMax(&st->peak_bits[n], (unsigned long long)__double_as_longlong(v));
-        } else if (pass == 1) {
-            if (v > 0.0 && (unsigned long long)__double_as_longlong(v) == st->peak_bits[n])
-                atomicMin(&st->donor[n], (unsigned long long)(cell_base + idx));
-        }
-    }
-}
-template <int NS>
-__global__ void k_repair_apply(hf_patch P, double* __restrict__ U, double vol, DevStatus* st) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)P.nx * P.ny) return;
-    const int i = (int)(idx % P.nx), j = (int)(idx / P.nx);
-    const int64_t g = P.offset + (int64_t)(j + P.ng) * P.pitch + (i + P.ng);
-    for (int n = 0; n < NS; ++n) {
-        const double v = U[g + n * P.comp_stride];
-        if (v >= 0.0) continue;
-        const double peak = __longlong_as_double((long long)st->peak_bits[n]);
-        if (!isfinite(v) || -v > 64.0 * 2.220446049250313e-16 * peak) {
-            atomicOr(&st->flags, ST_MATERIAL);
-            continue;
-        }
-        atomicAdd(&st->deficit[n], -v * vol);
-        atomicAdd(&st->repairs, 1ull);
-        U[g + n * P.comp_stride] = 0.0;
-    }
-}
-// Single thread: take each species' deficit from its donor cell.
-template <int NS>
-__global__ void k_donor_fix(const hf_patch* __restrict__ patches, int npatch, double* U, double vol, DevStatus* st) {
-    for (int n = 0; n < NS; ++n) {
-        const double d = st->deficit[n];
-        if (!(d > 0.0)) continue;
-        const unsigned long long cell = st->donor[n];
-        const double peak = __longlong_as_double((long long)st->peak_bits[n]);
-        if (cell == ~0ull || !(peak * vol > d)) { atomicOr(&st->flags, ST_MATERIAL); continue; }
-        int64_t base = 0;
-        for (int p = 0; p < npatch; ++p) {
-            const hf_patch& P = patches[p];
-            const int64_t nc = (int64_t)P.nx * P.ny;
-            if ((int64_t)cell < base + nc) {
-                const int64_t k = (int64_t)cell - base;
-                const int i = (int)(k % P.nx), j = (int)(k / P.nx);
-                U[P.offset + n * P.comp_stride + (int64_t)(j + P.ng) * P.pitch + (i + P.ng)] -= d / vol;
-                break;
-            }
-            base += nc;
-        }
-    }
-}
-cudaError_t launch_repair_scan(int ns, const hf_patch& P, const double* U, int64_t cell_base, int pass, DevStatus* st,
-                               cudaStream_t s, int64_t* launches) {
-    const int64_t n = (int64_t)P.nx * P.ny;
-    HF_DISPATCH(ns, k_repair_scan)<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, U, cell_base, pass, st);
-    ++*launches;
-    return cudaGetLastError();
-}
-cudaError_t launch_repair_apply(int ns, const hf_patch& P, double* U, double vol, DevStatus* st, cudaStream_t s,
-                                int64_t* launches) {
-    const int64_t n = (int64_t)P.nx * P.ny;
-    HF_DISPATCH(ns, k_repair_apply)<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, U, vol, st);
-    ++*launches;
-    return cudaGetLastError();
-}
-cudaError_t launch_donor_fix(int ns, const hf_patch* pd, int npatch, double* U, double vol, DevStatus* st,
-                             cudaStream_t s, int64_t* launches) {
-    HF_DISPATCH(ns, k_donor_fix)<<<1, 1, 0, s>>>(pd, npatch, U, vol, st);
     ++*launches;
     return cudaGetLastError();
 }

@@ -15,9 +15,6 @@ struct DevStatus {
     unsigned long long counter;    // work-queue head / generic counter
     unsigned long long coop_counter;  // head of the batched chemistry's cooperative queue
     unsigned long long steps;      // integrator steps (accepted + rejected)
-    double deficit[16];            // roundoff repair deficits per species
-    unsigned long long peak_bits[16];
-    unsigned long long donor[16];
     unsigned long long repairs;
     unsigned long long coop_cells;  // cells the batched chemistry took in groups of 8 lanes
     // Set when a step of a device-resident multi-step run failed; the step kernels of
@@ -99,12 +96,6 @@ cudaError_t launch_validate(int ns, const hf_patch& P, const double* U, int64_t 
                             cudaStream_t s, int64_t* launches);
 cudaError_t launch_cfl(int ns, const Level& L, const hf_patch& P, const double* U, DevStatus* st,
                        cudaStream_t s, int64_t* launches);
-cudaError_t launch_repair_scan(int ns, const hf_patch& P, const double* U, int64_t cell_base, int pass,
-                               DevStatus* st, cudaStream_t s, int64_t* launches);
-cudaError_t launch_repair_apply(int ns, const hf_patch& P, double* U, double vol, DevStatus* st,
-                                cudaStream_t s, int64_t* launches);
-cudaError_t launch_donor_fix(int ns, const hf_patch* patches_dev, int npatch, double* U, double vol,
-                             DevStatus* st, cudaStream_t s, int64_t* launches);
 cudaError_t launch_properties(int ns, const double* q, int64_t stride, int64_t count, double* p, double* a,
                               double* T, int32_t* status, DevStatus* st, cudaStream_t s, int64_t* launches);
 cudaError_t launch_hllc(int ns, const double* l, const double* r, const double* pl, const double* pr,

@@ -37,6 +37,17 @@ MARGIN = 0.03
 STEP_CANDIDATES = [CHEM_DEFAULT, (4, 3), (4, 5), (4, 7)]
 
 
+def pick(sweep, key, default=CHEM_DEFAULT, margin=MARGIN):
+    """The sweep entry to apply: the fastest by `key` when it is more than `margin` faster
+    than the `default` setting's entry, else the default's (the fastest when the sweep
+    has no default entry)."""
+    best = min(sweep, key=lambda r: r[key])
+    base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == tuple(default)]
+    if base and best[key] >= (1.0 - margin) * base[0][key]:
+        return base[0]
+    return best
+
+
 def get_chem_tuning(ctx):
     m, c = ctypes.c_int32(0), ctypes.c_int32(0)
     ctx.lib.hf_get_chem_tuning(ctypes.byref(m), ctypes.byref(c))
@@ -78,10 +89,7 @@ def tune_chemistry(ctx, X, dt, candidates=CHEM_CANDIDATES, apply=True):
             del field
     finally:
         set_chem_tuning(ctx, *before)
-    best = min(sweep, key=lambda r: r["ms"])
-    base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == CHEM_DEFAULT]
-    if base and best["ms"] > (1.0 - MARGIN) * base[0]["ms"]:
-        best = base[0]
+    best = pick(sweep, "ms")
     if apply:
         set_chem_tuning(ctx, best["blocks_per_sm"], best["coop_min_bucket"])
     return {"best": (best["blocks_per_sm"], best["coop_min_bucket"]), "sweep": sweep}
@@ -137,10 +145,7 @@ def tune_stepper(ctx, level, U, cfl, flux="plain", warm=2, steps=6, candidates=S
                           "coop_cells": c1["chem_coop_cells"] - c0["chem_coop_cells"]})
     finally:
         set_chem_tuning(ctx, *before)
-    best = min(sweep, key=lambda r: r["ms_per_step"])
-    base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == CHEM_DEFAULT]
-    if base and best["ms_per_step"] > (1.0 - MARGIN) * base[0]["ms_per_step"]:
-        best = base[0]
+    best = pick(sweep, "ms_per_step")
     if apply:
         set_chem_tuning(ctx, best["blocks_per_sm"], best["coop_min_bucket"])
     return {"best": (best["blocks_per_sm"], best["coop_min_bucket"]), "sweep": sweep}

@@ -21,7 +21,7 @@ def test_chemistry_tuner_applies_the_fastest_candidate(gpu):
         assert len(sweep) == len(tune.CHEM_CANDIDATES) and all(r["ms"] > 0 for r in sweep)
         best = min(sweep, key=lambda r: r["ms"])
         base = [r for r in sweep if (r["blocks_per_sm"], r["coop_min_bucket"]) == tune.CHEM_DEFAULT][0]
-        if best["ms"] > (1.0 - tune.MARGIN) * base["ms"]:
+        if best["ms"] >= (1.0 - tune.MARGIN) * base["ms"]:
             best = base  # the default stays unless a candidate beats it by the margin
         assert res["best"] == (best["blocks_per_sm"], best["coop_min_bucket"]) == tune.get_chem_tuning(gpu)
         # the cooperative phase runs for a low threshold and never for 16
@@ -62,7 +62,7 @@ def test_stepper_tuner_times_whole_steps(gpu):
         assert all(r["ms_per_step"] > 0 for r in sweep)
         assert sweep[0]["coop_cells"] == 0 and sweep[1]["coop_cells"] > 0
         base, other = sweep
-        want = (4, 3) if other["ms_per_step"] <= (1 - tune.MARGIN) * base["ms_per_step"] else tune.CHEM_DEFAULT
+        want = (4, 3) if other["ms_per_step"] < (1 - tune.MARGIN) * base["ms_per_step"] else tune.CHEM_DEFAULT
         assert res["best"] == want == tune.get_chem_tuning(gpu)
     finally:
         tune.set_chem_tuning(gpu, *default)
