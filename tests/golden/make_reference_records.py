@@ -1,7 +1,11 @@
 """Writes reference_records.json: the run outcomes that HyperFlow V3 records for its own
 checks (HyperFlow_V3/docs/case_checks.json and docs/amr_checks.json), reduced to the
-fields the oracle and GPU tests compare with; and reference_cases.json: the keys of its
-two smoke case configurations (cases/*/smoke.json) that the case loader reads.  Run
+fields the oracle and GPU tests compare with; reference_cases.json: the keys of its
+two smoke case configurations (cases/*/smoke.json) that the case loader reads; and
+h2li_mechanism.json: the numbers of its mechanism file (H2_Li.yaml: species order,
+compositions, NASA7 ranges and coefficients; each reaction's equation, type, rate
+parameters as written, efficiencies, Troe parameters), read by a parser of its own so
+that a test can check the generated kernel tables against them independently.  Run
 where the reference tree is present, with its HyperFlow_V3 directory as the one required
 argument:
 
@@ -34,6 +38,66 @@ CASE_KEYS = {"problem", "T0", "P0", "u0", "v0", "hot_T", "hot_P", "hotspot_width
              "center", "radius", "sigma", "amplitude", "initial_subsamples", "interface"}
 
 
+def _flow_map(text):
+    """'{A: 1.0, b: -0.5, Ea: 3.0 cal/mol}' -> {"A": 1.0, "b": -0.5, "Ea": 3.0, "Ea_unit": "cal/mol"}"""
+    body = text.strip()
+    assert body[0] == "{" and body[-1] == "}", text
+    out = {}
+    for item in body[1:-1].split(","):
+        k, v = item.split(":", 1)
+        parts = v.split()
+        out[k.strip()] = float(parts[0])
+        if len(parts) > 1:
+            out[k.strip() + "_unit"] = " ".join(parts[1:])
+    return out
+
+
+def mechanism(path):
+    text = open(path).read()
+    lines = text.splitlines()
+    phase_species = None
+    species, reactions = [], []
+    section = None
+    i = 0
+    while i < len(lines):
+        line = lines[i]
+        stripped = line.strip()
+        if line.startswith("phases:"):
+            section = "phases"
+        elif line.startswith("species:"):
+            section = "species"
+        elif line.startswith("reactions:"):
+            section = "reactions"
+        elif section == "phases" and stripped.startswith("species:") and phase_species is None:
+            phase_species = [t.strip() for t in stripped.split("[", 1)[1].rstrip("]").split(",")]
+        elif section == "species" and line.startswith("- name:"):
+            species.append({"name": stripped.split(":", 1)[1].strip(), "nasa7": []})
+        elif section == "species" and stripped.startswith("composition:"):
+            species[-1]["composition"] = _flow_map(stripped.split(":", 1)[1])
+        elif section == "species" and stripped.startswith("temperature-ranges:"):
+            species[-1]["temperature_ranges"] = [float(t) for t in stripped.split("[", 1)[1].rstrip("]").split(",")]
+        elif section == "species" and stripped.startswith("- [") and "temperature_ranges" in species[-1]:
+            buf = stripped[2:]
+            while "]" not in buf:
+                i += 1
+                buf += " " + lines[i].strip()
+            species[-1]["nasa7"].append([float(t) for t in buf.strip("[] ").split(",")])
+        elif section == "reactions" and line.startswith("- equation:"):
+            reactions.append({"equation": stripped.split(":", 1)[1].strip(), "type": "elementary"})
+        elif section == "reactions" and reactions and ":" in stripped:
+            key, val = stripped.split(":", 1)
+            val = val.strip()
+            if key in ("rate-constant", "high-P-rate-constant", "low-P-rate-constant", "efficiencies", "Troe"):
+                reactions[-1][key] = _flow_map(val)
+            elif key == "type":
+                reactions[-1]["type"] = val
+            elif key == "duplicate":
+                reactions[-1]["duplicate"] = val == "true"
+        i += 1
+    return {"source": "HyperFlow_V3/H2_Li.yaml", "phase_species": phase_species, "species": species,
+            "reactions": reactions}
+
+
 def main(root):
     out = {}
     for (name, group, case), keys in FIELDS.items():
@@ -54,6 +118,11 @@ def main(root):
     path = os.path.join(here, "reference_cases.json")
     with open(path, "w") as f:
         json.dump(cases, f, indent=1, sort_keys=True)
+        f.write("\n")
+    print("wrote", path)
+    path = os.path.join(here, "h2li_mechanism.json")
+    with open(path, "w") as f:
+        json.dump(mechanism(os.path.join(root, "H2_Li.yaml")), f, indent=1)
         f.write("\n")
     print("wrote", path)
 
