@@ -175,6 +175,29 @@ def _oracle(ns):
     return oracle
 
 
+def flux_roofline(ff, nv, cells, flux_ms_per_step, fp64_peak, hbm_gbs):
+    """The flux path's roofline over a step (4 Euler stages, 2 Heun combines): the
+    oracle's counted FP64 flops per cell-step (ff = oracle.flux_flops of a face stencil:
+    2 faces per cell-stage, one cell update and validation per stage, a combine in each
+    Heun stage) and the algorithmic HBM bytes per cell-step (stage 1 reads U and writes
+    U1, stage 2 reads U1 and U_old and writes U: 5 state transfers per flow half-step)
+    over the measured flux time per step; the bound is the larger fraction."""
+    flops = 4 * (2 * ff["face"] + ff["cell"]) + 2 * ff["combine"]
+    nbytes = 2 * (2 + 3) * nv * 8
+    sec = flux_ms_per_step * 1e-3
+    gf = flops * cells / sec / 1e9
+    gb = nbytes * cells / sec / 1e9
+    return {"kernels": "k_face_plain (x, y) + k_update_plain, k_fill, k_cfl of a step",
+            "bound": "fp64" if gf / fp64_peak >= gb / hbm_gbs else "hbm", "ms_per_step": flux_ms_per_step,
+            "fp64": {"flops_per_cell_step": flops, "achieved": gf, "peak": fp64_peak, "unit": "GFLOP/s",
+                     "frac": gf / fp64_peak, "per_face": ff["face"], "per_cell_update": ff["cell"],
+                     "per_combine": ff["combine"],
+                     "source": "the oracle's flux functions on a counting scalar, 3 UV Newton iterations per "
+                               "EOS solve from 1000 K, at a subsonic face of the fresh gas (HLLC star state)"},
+            "hbm": {"bytes_per_cell_step": nbytes, "achieved": gb, "peak": hbm_gbs, "unit": "GB/s",
+                    "frac": gb / hbm_gbs}}
+
+
 def cpu_window(steps, warm, rows=STRIP_ROWS, nx=NX, threads=0, serial_steps=0, cfl=0.5):
     """The oracle's Strang steps on a periodic strip (nx x rows) of the 2D detonation: warm
     untimed steps, then `steps` timed ones, every loop on all host threads (OpenMP flux,
@@ -729,6 +752,10 @@ def run_ours(args):
             "note": "the chemistry kernel is FP64-pipe bound, not HBM bound: the HBM fraction is reported per the "
                     "contract, the fp64 object (algorithmic FP64 work of the launch's input over its time) is the "
                     "binding roof"}
+    # the flux path's roofline: a subsonic face stencil of the fresh gas (x direction)
+    mid = max(0, min(args.nx // 2, args.nx - 4))
+    ff = _oracle(nv - 3).flux_flops(U0[:, 0, mid:mid + 4].T, 0, 3)
+    roof["flux"] = flux_roofline(ff, nv, cells, tm["flux"][0] / args.steps, fp64_peak, hbm)
     accuracy = None
     if not args.no_cpu:
         # error of the GPU results against the tight FP64 oracle (rtol 1e-12,

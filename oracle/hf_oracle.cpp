@@ -92,6 +92,7 @@ inline double xfabs(double x) { return std::fabs(x); }
 inline double xmax(double a, double b) { return std::max(a, b); }
 inline double xmin(double a, double b) { return std::min(a, b); }
 inline bool xfinite(double x) { return std::isfinite(x); }
+inline double xcopysign(double a, double b) { return std::copysign(a, b); }
 inline Fl xexp(Fl x) { ++g_fl_trans; return Fl(std::exp(x.v)); }
 inline Fl xlog(Fl x) { ++g_fl_trans; return Fl(std::log(x.v)); }
 inline Fl xlog10(Fl x) { ++g_fl_trans; return Fl(std::log10(x.v)); }
@@ -101,6 +102,7 @@ inline Fl xfabs(Fl x) { return Fl(std::fabs(x.v)); }
 inline Fl xmax(Fl a, Fl b) { return Fl(std::max(a.v, b.v)); }
 inline Fl xmin(Fl a, Fl b) { return Fl(std::min(a.v, b.v)); }
 inline bool xfinite(Fl x) { return std::isfinite(x.v); }
+inline Fl xcopysign(Fl a, Fl b) { return Fl(std::copysign(a.v, b.v)); }
 // Newton iterations of the UV inversion when counting (a fixed count makes the flop
 // figure independent of the state): 0 = iterate to convergence
 thread_local int g_fixed_newton = 0;
@@ -170,58 +172,66 @@ bool solve_T(const F* Y, F e, F& T) {
     return fixed > 0;
 }
 
-double density(const double* q) {
-    double r = 0;
+// The flux-path functions below are templates on the scalar type as well (double for
+// the oracle, Fl for the flux path's flop count, or_flux_flops).
+template <class F>
+F density(const F* q) {
+    F r = 0;
     for (int k = 0; k < NS; ++k) r += q[k];
     return r;
 }
-double internal_energy(const double* q) {
-    const double rho = density(q);
-    const double u = q[MX()] / rho, v = q[MY()] / rho;
+template <class F>
+F internal_energy(const F* q) {
+    const F rho = density(q);
+    const F u = q[MX()] / rho, v = q[MY()] / rho;
     return q[EN()] / rho - 0.5 * (u * u + v * v);
 }
 
-struct Props { double p, a, T; };
+template <class F>
+struct PropsT { F p, a, T; };
+using Props = PropsT<double>;
 
 // physics.cpp:4-15.  T_guess is the starting temperature of the UV Newton solve.
-bool properties(const double* q, Props& s, double T_guess = 1000.0) {
-    for (int n = 0; n < NV(); ++n) if (!std::isfinite(q[n])) return false;
-    const double rho = density(q);
+template <class F>
+bool properties(const F* q, PropsT<F>& s, F T_guess = F(1000.0)) {
+    for (int n = 0; n < NV(); ++n) if (!xfinite(q[n])) return false;
+    const F rho = density(q);
     if (!(rho > 0)) return false;
     for (int k = 0; k < NS; ++k) if (q[k] < 0) return false;
-    double Y[NS_MAX];
+    F Y[NS_MAX];
     for (int k = 0; k < NS; ++k) Y[k] = q[k] / rho;
-    double T = T_guess;
+    F T = T_guess;
     if (!solve_T(Y, internal_energy(q), T)) return false;
-    const double z = inv_mmw(Y);
-    const double cv = mix_cv(Y, T), cp = cv + R * z;
+    const F z = inv_mmw(Y);
+    const F cv = mix_cv(Y, T), cp = cv + R * z;
     s.T = T;
     s.p = rho * R * T * z;
-    s.a = std::sqrt(cp / cv * R * T * z);
-    return s.T > 0 && s.p > 0 && s.a > 0 && std::isfinite(s.a);
+    s.a = xsqrt(cp / cv * R * T * z);
+    return s.T > 0 && s.p > 0 && s.a > 0 && xfinite(s.a);
 }
 
 // physics.cpp:17-38
-void hllc(const double* l, const double* r, int n, Props pl, Props pr, double* out) {
+template <class F>
+void hllc(const F* l, const F* r, int n, PropsT<F> pl, PropsT<F> pr, F* out) {
     const int E = EN();
-    const double rl = density(l), rr = density(r), ul = l[n] / rl, ur = r[n] / rr;
-    const double sl = std::min(ul - pl.a, ur - pr.a), sr = std::max(ul + pl.a, ur + pr.a);
-    auto flux = [&](const double* q, double v, double p, double* f) {
+    const F rl = density(l), rr = density(r), ul = l[n] / rl, ur = r[n] / rr;
+    const F sl = xmin(ul - pl.a, ur - pr.a), sr = xmax(ul + pl.a, ur + pr.a);
+    auto flux = [&](const F* q, F v, F p, F* f) {
         for (int m = 0; m < NV(); ++m) f[m] = v * q[m];
         f[n] += p;
         f[E] += p * v;
     };
     if (sl >= 0) { flux(l, ul, pl.p, out); return; }
     if (sr <= 0) { flux(r, ur, pr.p, out); return; }
-    const double dl = rl * (sl - ul), dr = rr * (sr - ur);
-    const double sm = (pr.p - pl.p + dl * ul - dr * ur) / (dl - dr);
+    const F dl = rl * (sl - ul), dr = rr * (sr - ur);
+    const F sm = (pr.p - pl.p + dl * ul - dr * ur) / (dl - dr);
     const bool left = sm >= 0;
-    const double* q = left ? l : r;
-    const double v = left ? ul : ur, s = left ? sl : sr, p = left ? pl.p : pr.p;
-    double star[MAXV], f[MAXV];
-    const double scale = (s - v) / (s - sm);
+    const F* q = left ? l : r;
+    const F v = left ? ul : ur, s = left ? sl : sr, p = left ? pl.p : pr.p;
+    F star[MAXV], f[MAXV];
+    const F scale = (s - v) / (s - sm);
     for (int m = 0; m < NV(); ++m) star[m] = q[m] * scale;
-    const double rs = density(star);
+    const F rs = density(star);
     star[n] = rs * sm;
     star[E] += rs * (sm - v) * (sm + p / (density(q) * (s - v)));
     flux(q, v, p, f);
@@ -229,8 +239,22 @@ void hllc(const double* l, const double* r, int n, Props pl, Props pr, double* o
 }
 
 // physics.cpp:40-44
-double minmod1(double x, double y) {
-    return x * y > 0 ? std::copysign(std::min(std::fabs(x), std::fabs(y)), x) : 0.;
+template <class F>
+F minmod1(F x, F y) {
+    return x * y > 0 ? xcopysign(xmin(xfabs(x), xfabs(y)), x) : F(0.);
+}
+// MUSCL face states of the stage (BlockAMR.cpp:218-219) from the 4-cell stencil
+template <class F>
+void muscl_face(const F* qa, const F* qb, const F* qc, const F* qd, F* L, F* Rr) {
+    for (int n = 0; n < NV(); ++n) {
+        L[n] = qb[n] + 0.5 * minmod1(qb[n] - qa[n], qc[n] - qb[n]);
+        Rr[n] = qc[n] - 0.5 * minmod1(qc[n] - qb[n], qd[n] - qc[n]);
+    }
+}
+// flux divergence update of one cell (BlockAMR.cpp:234-243)
+template <class F>
+void cell_update(const F* q, const F* fl, const F* fr, const F* fb, const F* ft, F cx, F cy, F* out) {
+    for (int n = 0; n < NV(); ++n) out[n] = q[n] - cx * (fr[n] - fl[n]) - cy * (ft[n] - fb[n]);
 }
 
 // ---------------------------------------------------------------- kinetics
@@ -999,6 +1023,36 @@ void or_chem_flops(double rho, double e, const double* y, double T, int newton, 
     g_fixed_newton = 0;
 }
 
+// FP64 work of the flux path as this restatement does it (flops: add, sub, mul, div,
+// sqrt), with every UV inversion taking exactly `newton` iterations from the stage's
+// starting guess of 1000 K.  From a 4-cell stencil along direction dir (AoS, NV each):
+// out[0] the flops of one face (MUSCL on both sides, the EOS of the two face states,
+// HLLC), out[1] of one cell's flux-divergence update and validation (one EOS), out[2]
+// of one cell's Heun combine, out[3] the transcendental calls of a face.
+void or_flux_flops(const double* stencil, int dir, int newton, double* out) {
+    const int nv = NV();
+    Fl q[4][MAXV], L[MAXV], Rr[MAXV], f[MAXV], o[MAXV];
+    for (int c = 0; c < 4; ++c)
+        for (int n = 0; n < nv; ++n) q[c][n] = stencil[c * nv + n];
+    g_fixed_newton = newton;
+    g_fl_ops = g_fl_trans = 0;
+    muscl_face(q[0], q[1], q[2], q[3], L, Rr);
+    PropsT<Fl> pl, pr, pc;
+    properties(L, pl);
+    properties(Rr, pr);
+    hllc(L, Rr, dir == 0 ? MX() : MY(), pl, pr, f);
+    out[0] = (double)g_fl_ops;
+    out[3] = (double)g_fl_trans;
+    g_fl_ops = 0;
+    cell_update(q[1], f, f, f, f, Fl(0.1), Fl(0.1), o);
+    properties(o, pc);
+    out[1] = (double)g_fl_ops;
+    g_fl_ops = 0;
+    for (int n = 0; n < nv; ++n) o[n] = 0.5 * q[1][n] + 0.5 * o[n];
+    out[2] = (double)g_fl_ops;
+    g_fixed_newton = 0;
+}
+
 // Objective (OBJ_*) of count AoS cells over nsub adaptive chemistry calls of dt
 // each; mult: NR rate multipliers (null = 1).  Returns -1, or the lowest failing cell.
 int64_t or_chem_objective(const double* U0, int64_t count, double dt, int nsub, int obj, double dT, double rtol,
@@ -1183,10 +1237,7 @@ int or_euler_stage(const or_grid* g, const double* Ug, double* Uout, double h, i
                 qc[n] = atc(g, Ug, i, j, n);
                 qd[n] = atc(g, Ug, i + di, j + dj, n);
             }
-            for (int n = 0; n < nv; ++n) {
-                L[n] = qb[n] + 0.5 * minmod1(qb[n] - qa[n], qc[n] - qb[n]);
-                Rr[n] = qc[n] - 0.5 * minmod1(qc[n] - qb[n], qd[n] - qc[n]);
-            }
+            muscl_face(qa, qb, qc, qd, L, Rr);
             if (first_order) for (int n = 0; n < nv; ++n) { L[n] = qb[n]; Rr[n] = qc[n]; }
             Props pl, pr;
             if (!properties(L, pl)) { std::copy(qb, qb + nv, L); }
@@ -1215,8 +1266,10 @@ int or_euler_stage(const or_grid* g, const double* Ug, double* Uout, double h, i
         const double* fr = fl + nv;
         const double* fb = &fy[((size_t)j * nx + i) * nv];
         const double* ft = &fy[((size_t)(j + 1) * nx + i) * nv];
-        for (int n = 0; n < nv; ++n)
-            at(g, Uout, i, j, n) = atc(g, Ug, i, j, n) - cx * (fr[n] - fl[n]) - cy * (ft[n] - fb[n]);
+        double q[MAXV], o[MAXV];
+        for (int n = 0; n < nv; ++n) q[n] = atc(g, Ug, i, j, n);
+        cell_update(q, fl, fr, fb, ft, cx, cy, o);
+        for (int n = 0; n < nv; ++n) at(g, Uout, i, j, n) = o[n];
     }
     if (fx_out) std::copy(fx.begin(), fx.end(), fx_out);
     if (fy_out) std::copy(fy.begin(), fy.end(), fy_out);

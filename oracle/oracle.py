@@ -65,6 +65,7 @@ def lib():
         L.or_chem_batch_stats.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_int, _lp, _lp]
         L.or_chem_flops.argtypes = [ctypes.c_double, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_int, _dp]
+        L.or_flux_flops.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
         L.or_chem_batch.restype = ctypes.c_int64
         L.or_chem_batch.argtypes = [_dp, ctypes.c_int64, ctypes.c_double, _dp, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int, _lp]
@@ -239,6 +240,17 @@ def chem_flops(u, newton=3):
     out = np.zeros(4)
     lib().or_chem_flops(rho, e, _p(y), T, int(newton), _p(out))
     return tuple(out)
+
+
+def flux_flops(stencil, direction=0, newton=3):
+    """FP64 flops of the flux path at a 4-cell stencil (4 x NV AoS states along
+    `direction`), every UV inversion fixed at `newton` iterations from 1000 K:
+    {"face": one face (MUSCL, 2 EOS, HLLC), "cell": one cell's update and validation,
+    "combine": one cell's Heun combine, "face_transcendental": calls per face}."""
+    st = np.ascontiguousarray(np.asarray(stencil, dtype=np.float64).reshape(4, -1))
+    out = np.zeros(4)
+    lib().or_flux_flops(_p(st), int(direction), int(newton), _p(out))
+    return {"face": out[0], "cell": out[1], "combine": out[2], "face_transcendental": out[3]}
 
 
 def set_flux_threads(threads=1):
